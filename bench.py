@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 onesweep LSD radix sort (libgbsort.so, C ABI).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2b|c1|c2a|c3a|c3b]
+                    [--impl gbsort|reference]
+
+One step = one sort (histogram upsweep + one onesweep pass per key byte) of a
+fresh batch of synthetic keys already resident in HBM.  Before each step the
+next batch is generated on the device (splitmix64 stream, new seed) and a
+512 MiB buffer is written to flush L2; CUDA events on the sort's stream time
+the sort alone, and `value` = keys sorted / summed event time.  The K timed
+steps are bracketed by a barrier + torch.cuda.synchronize() on both sides.
+
+Default workload (the headline): 2^28 uint32 keys, uniform full range,
+ascending, keys only, 8-bit digits / 4 passes.  Other --config values are the
+other configurations of the reference's benchmark table.
+
+Extra keys on the JSON line:
+  roofline      the dominant kernel (the onesweep pass): algorithmic bytes per
+                launch (n * 2 * (key + value bytes)) / its mean CUDA-event
+                duration, against MEASURED_PEAKS.json's HBM copy bandwidth;
+                `traffic` = ncu dram bytes per launch from profiles/ when a
+                capture of this workload is committed there
+  sort_roofline the whole sort: (K + P*2*(K+V)) bytes per key / sort time
+  e2e           same metric through gbsort_sort_host with pinned HOST buffers,
+                H2D + sort + D2H inside the timed region
+  cpu_baseline  the CPU oracle (std::stable_sort of twiddled keys, 1 thread)
+                on a bounded sample of the same workload (rank 0, N=1 only)
+  clocks        nvidia-smi samples taken during the timed region
+--impl reference times the reference path's CPU implementation (the oracle
+port: parallel stable sort on every host core) on samples of the workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "cuda-fast-sort_gb300")
+sys.path.insert(0, PKG)
+
+CONFIGS = {
+    "c2b": dict(key="u32", n=1 << 28, dist=0, vb=0, desc=False,
+                workload="u32 keys-only, n=2^28, uniform full-range (splitmix64), ascending, 8-bit radix x 4 passes"),
+    "c1": dict(key="u32", n=1 << 20, dist=0, vb=0, desc=False,
+               workload="u32 keys-only, n=2^20, uniform full-range (splitmix64), ascending, 8-bit radix x 4 passes"),
+    "c2a": dict(key="f32", n=1 << 28, dist=1, vb=4, desc=False,
+                workload="f32 keys N(0,1) with 1% -0.0 / 0.1% +-inf / 0.01% NaN + u32 index values, n=2^28, "
+                         "ascending"),
+    "c3a": dict(key="u64", n=1 << 27, dist=2, vb=8, desc=True,
+                workload="u64 keys (upper 32 bits from 256 values) + u64 index values, n=2^27, descending"),
+    "c3b": dict(key="u128", n=1 << 26, dist=0, vb=0, desc=True,
+                workload="u128 keys (two uniform 64-bit halves), keys-only, n=2^26, descending"),
+}
+KEY_BYTES = {"u32": 4, "f32": 4, "u64": 8, "u128": 16}
+FALLBACK_HBM_GBS = 6800.0
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic(config: str):
+    """dram bytes per pass launch from a committed ncu summary, if any."""
+    path = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        e = d.get(config)
+        return None if e is None else e
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi -lms 200 in the background while the timed region runs."""
+
+    def __init__(self, gpu_index: int):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(gpu_index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.rows.append([x.strip() for x in ln.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for i, nm in enumerate(names):
+                    if r[5 + i].lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("GBSORT_BENCH_BACKEND") != "gloo" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_bits(cfg, n_sample: int, seed: int):
+    from gbsort import gen
+
+    return gen.generate(cfg["dist"], KEY_BYTES[cfg["key"]], n_sample, seed)
+
+
+def run_cpu_oracle(cfg, n_sample: int, threads: int, reps_min: int, budget_s: float):
+    """Times the oracle (test infrastructure, the CPU checker) on a sample."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import _oracle
+
+    oracle = _oracle.load()
+    raw = cpu_sample_bits(cfg, n_sample, seed=99)
+    vals = np.arange(n_sample, dtype=np.uint32 if cfg["vb"] == 4 else np.uint64) if cfg["vb"] else None
+    times = []
+    t_start = time.time()
+    while len(times) < reps_min or (time.time() - t_start < budget_s and len(times) < 50):
+        t0 = time.perf_counter()
+        oracle.sort(cfg["key"], raw, cfg["desc"], vals, threads=threads)
+        times.append(time.perf_counter() - t0)
+    return n_sample / statistics.mean(times) / 1e9, times
+
+
+def bench_reference(args, cfg, world, rank):
+    """The reference path's CPU implementation (oracle port), all host cores."""
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import _oracle
+
+    oracle = _oracle.load()
+    # size the per-step sample so the whole run stays within ~2 minutes
+    probe_n = min(cfg["n"], 1 << 22)
+    probe = cpu_sample_bits(cfg, probe_n, seed=6)
+    t0 = time.perf_counter()
+    oracle.sort(cfg["key"], probe, cfg["desc"], None, threads=cores)
+    per_key = (time.perf_counter() - t0) / probe_n * (2.0 if cfg["vb"] else 1.0)
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    n_sample = int(min(cfg["n"], 1 << 26, max(1 << 20, budget / max(per_key, 1e-12))))
+    raw = cpu_sample_bits(cfg, n_sample, seed=7)
+    vals = np.arange(n_sample, dtype=np.uint32 if cfg["vb"] == 4 else np.uint64) if cfg["vb"] else None
+    for _ in range(args.warmup):
+        oracle.sort(cfg["key"], raw, cfg["desc"], vals, threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.sort(cfg["key"], raw, cfg["desc"], vals, threads=cores)
+        times.append(time.perf_counter() - t0)
+    value = n_sample / statistics.mean(times) / 1e9
+    sample = f"{n_sample} keys of the same distribution per step (libstdc++ parallel stable_sort of twiddled keys)"
+    line = {
+        "impl": "reference", "metric": "sort throughput", "value": round(value, 4), "unit": "Gkeys/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * statistics.mean(times), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": cfg["key"], "data": "synthetic",
+        "config": {"workload": cfg["workload"], "sample_keys": n_sample, "flush": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_gbsort(args, cfg, world, rank, local):
+    import torch
+
+    import gbsort
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    kt, n, vb, desc = cfg["key"], cfg["n"], cfg["vb"], cfg["desc"]
+    kbytes = KEY_BYTES[kt]
+    passes = kbytes
+    # bench batches: two key buffers (+ values) used alternately; regenerated each step
+    keys = [torch.empty(n * kbytes, dtype=torch.uint8, device=dev) for _ in range(2)]
+    vals = [torch.empty(n * vb, dtype=torch.uint8, device=dev) for _ in range(2)] if vb else [None, None]
+    tb = gbsort.temp_bytes(kt, n, vb)
+    ws = torch.empty(tb, dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    seed_base = 1000 * (rank + 1)
+
+    def prepare(slot, seed):
+        gbsort.generate(cfg["dist"], kbytes, keys[slot], n, seed, stream)
+        if vb:
+            gbsort.generate(3, vb, vals[slot], n, 0, stream)  # values = original index
+        flush.fill_(seed & 0xFF)  # evict the fresh batch from L2
+
+    def run(slot):
+        gbsort.sort(keys[slot], n, kt, ws, tb, values=vals[slot], value_bytes=vb, descending=desc, stream=stream)
+
+    for w in range(args.warmup):
+        prepare(w & 1, seed_base + w)
+        run(w & 1)
+    torch.cuda.synchronize()
+    st = gbsort.workspace_status(kt, n, ws, vb, stream)
+    if st != gbsort.OK:
+        raise RuntimeError(f"warm-up sort reported {gbsort.status_string(st)}")
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local) if rank == 0 else None
+    barrier(world)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        slot = i & 1
+        prepare(slot, seed_base + args.warmup + i)
+        ev[i][0].record(stream)
+        run(slot)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop() if clocks else None
+    st = gbsort.workspace_status(kt, n, ws, vb, stream)
+    if st != gbsort.OK:
+        raise RuntimeError(f"timed sort reported {gbsort.status_string(st)}")
+    sort_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = max_over_ranks(world, sum(sort_ms))
+    value = world * args.steps * n / (total_ms / 1e3) / 1e9
+
+    # sanity check of the last timed batch on the device (ascending u32 only)
+    ok = None
+    if kt == "u32" and not desc and not vb:
+        k = keys[(args.steps - 1) & 1].view(torch.int32).to(torch.int64) & 0xFFFFFFFF
+        ok = bool((k[1:] >= k[:-1]).all().item())
+        del k
+
+    # per-kernel event times (dominant kernel: the pass) on fresh batches
+    hbm, peak_kind = peaks()
+    per_kernel = []
+    for r in range(3):
+        prepare(r & 1, 77 + r)
+        per_kernel.append(gbsort.sort_timed(keys[r & 1], n, kt, ws, tb, values=vals[r & 1], value_bytes=vb,
+                                            descending=desc, stream=stream))
+    ups_ms = statistics.mean(p[0] for p in per_kernel)
+    pass_ms = statistics.mean(statistics.mean(p[1:]) for p in per_kernel)
+    pass_bytes = n * 2 * (kbytes + vb)
+    achieved = pass_bytes / (pass_ms / 1e3) / 1e9
+    traffic = committed_traffic(args.config)
+    sort_bytes = n * (kbytes + passes * 2 * (kbytes + vb))
+    mean_sort_ms = total_ms / args.steps
+    roofline = {"bound": "hbm", "kernel": "onesweep_pass_kernel", "achieved": round(achieved, 1),
+                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s", "algorithmic_bytes_per_launch": pass_bytes,
+                "mean_launch_ms": round(pass_ms, 4), "upsweep_ms": round(ups_ms, 4)}
+    sort_roofline = {"bytes_per_key": kbytes + passes * 2 * (kbytes + vb), "achieved": round(
+        sort_bytes / (mean_sort_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+        "frac": round(sort_bytes / (mean_sort_ms / 1e3) / 1e9 / hbm, 4)}
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    e2e = None
+    if rank == 0 or world > 1:
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        hbytes = n * kbytes
+        h_src = torch.empty(hbytes, dtype=torch.uint8, pin_memory=True)
+        h_work = torch.empty(hbytes, dtype=torch.uint8, pin_memory=True)
+        hv_src = torch.empty(n * vb, dtype=torch.uint8, pin_memory=True) if vb else None
+        hv_work = torch.empty(n * vb, dtype=torch.uint8, pin_memory=True) if vb else None
+        prepare(0, 4242)
+        h_src.copy_(keys[0])
+        if vb:
+            hv_src.copy_(vals[0])
+        dbytes = gbsort.host_buffer_bytes(kt, n, vb)
+        dbuf = torch.empty(dbytes, dtype=torch.uint8, device=dev)
+        e2e_t = []
+        for _ in range(e2e_steps + 1):
+            h_work.copy_(h_src)
+            if vb:
+                hv_work.copy_(hv_src)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            gbsort.sort_host(h_work, n, kt, dbuf, dbytes, h_values=hv_work, value_bytes=vb, descending=desc,
+                             stream=stream)
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_t = e2e_t[1:]  # first call is a warm-up
+        e2e = {"value": round(n / statistics.mean(e2e_t) / 1e9, 4), "unit": "Gkeys/s",
+               "h2d_bytes_per_step": n * (kbytes + vb), "d2h_bytes_per_step": n * (kbytes + vb),
+               "steps": e2e_steps, "ms_per_step": round(1000 * statistics.mean(e2e_t), 3),
+               "api": "gbsort_sort_host (pinned host buffers)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n_sample = min(n, 1 << 24)
+        v, times = run_cpu_oracle(cfg, n_sample, threads=1, reps_min=1, budget_s=args.cpu_seconds)
+        cpu = {"value": round(v, 5), "unit": "Gkeys/s", "cores": 1, "kind": "port",
+               "sample": f"{n_sample} keys of the same distribution, std::stable_sort of twiddled keys, "
+                         f"{len(times)} reps ({sum(times):.1f} s)"}
+
+    if rank != 0:
+        return
+    plan = gbsort.plan(kt, n, vb)
+    line = {
+        "metric": "sort throughput (Gkeys/s) and HBM roofline fraction", "value": round(value, 3),
+        "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": kt, "data": "synthetic",
+        "config": {"workload": cfg["workload"], "n": n, "key": kt, "value_bytes": vb, "descending": desc,
+                   "passes": passes, "radix_bits": 8, "tile_items": plan.tile_items,
+                   "threads": plan.threads, "items_per_thread": plan.items_per_thread,
+                   "pass_ctas": plan.pass_ctas, "status_word_bytes": plan.status_word_bytes,
+                   "flush": "inputs (>= 1 GiB) larger than L2, plus a 512 MiB L2 flush before every step",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "wall_ms_per_step_incl_input_generation": round(1000 * wall / args.steps, 3)},
+        "roofline": roofline,
+        "sort_roofline": sort_roofline,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": args.steps * (passes + 2 + (1 if vb else 0)),
+        "gpu_launches_note": "per step: generate (+values) + upsweep + one pass per key byte; plus one memset node",
+        "sorted_check": ok,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", default="c2b", choices=sorted(CONFIGS))
+    ap.add_argument("--impl", default="gbsort", choices=["gbsort", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)  # timing rule: at least 3 warm-up steps
+    world, rank, local = dist_init()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        bench_reference(args, cfg, world, rank)
+    else:
+        bench_gbsort(args, cfg, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

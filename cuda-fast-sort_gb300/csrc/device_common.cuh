@@ -1,0 +1,257 @@
+// device_common.cuh — key bit types, twiddling, status-word codec, TMA /
+// mbarrier / memory-order helpers and bounded waits for the sm_103a sort.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbsort {
+
+using u128 = unsigned __int128;
+
+// Key kinds of the twiddle (reference: include/rsort/detail/tuning.cuh:352-384).
+enum KeyKind : int { KIND_UNSIGNED = 0, KIND_SIGNED = 1, KIND_FLOAT = 2 };
+
+// Error bits of the workspace error word.
+enum : uint32_t { ERRBIT_TIMEOUT = 1u, ERRBIT_BOUNDS = 2u };
+
+// Device-side bounds checks on staging ranks and scatter positions: a failed
+// check records ERRBIT_BOUNDS and skips the access instead of faulting.
+#ifndef GBSORT_BOUNDS_CHECK
+#define GBSORT_BOUNDS_CHECK 1
+#endif
+
+// After a wait ran out, copies still in flight are drained for at most this
+// long before a CTA leaves (a bulk copy from valid memory lands in microseconds).
+constexpr uint64_t DRAIN_LIMIT_NS = 1000000000ull;
+
+template <int KB> struct KeyBits;
+template <> struct KeyBits<1> { using U = uint8_t; };
+template <> struct KeyBits<2> { using U = uint16_t; };
+template <> struct KeyBits<4> { using U = uint32_t; };
+template <> struct KeyBits<8> { using U = uint64_t; };
+template <> struct KeyBits<16> { using U = u128; };
+
+// Value payloads are moved as raw bytes of these types.
+struct alignas(16) Val16 { uint64_t lo, hi; };
+template <int VB> struct ValBits { using V = uint8_t; };  // VB == 0: unused
+template <> struct ValBits<1> { using V = uint8_t; };
+template <> struct ValBits<2> { using V = uint16_t; };
+template <> struct ValBits<4> { using V = uint32_t; };
+template <> struct ValBits<8> { using V = uint64_t; };
+template <> struct ValBits<16> { using V = Val16; };
+
+// Order-preserving map of a key's bits to an unsigned value (and back).
+// kind/desc are launch-uniform, so the selects compile to predicated ops.
+template <class U>
+__device__ __forceinline__ U twiddle_in(U b, int kind, int desc) {
+    const U sign = U(U(1) << (8 * sizeof(U) - 1));
+    const U base = (kind == KIND_UNSIGNED) ? U(0) : sign;
+    const bool neg_float = (kind == KIND_FLOAT) && ((b & sign) != U(0));
+    U x = U(b ^ (neg_float ? U(~U(0)) : base));
+    return desc ? U(~x) : x;
+}
+
+template <class U>
+__device__ __forceinline__ U twiddle_out(U t, int kind, int desc) {
+    const U sign = U(U(1) << (8 * sizeof(U) - 1));
+    const U base = (kind == KIND_UNSIGNED) ? U(0) : sign;
+    U y = desc ? U(~t) : t;
+    const bool was_neg_float = (kind == KIND_FLOAT) && ((y & sign) == U(0));
+    return U(y ^ (was_neg_float ? U(~U(0)) : base));
+}
+
+// 8-bit digit `pass` (0 = least significant byte) of a twiddled key.
+__device__ __forceinline__ uint32_t digit_of(uint8_t x, int) { return x; }
+__device__ __forceinline__ uint32_t digit_of(uint16_t x, int pass) {
+    return __byte_perm(uint32_t(x), 0u, 0x4440u | uint32_t(pass));
+}
+__device__ __forceinline__ uint32_t digit_of(uint32_t x, int pass) {
+    return __byte_perm(x, 0u, 0x4440u | uint32_t(pass));
+}
+__device__ __forceinline__ uint32_t digit_of(uint64_t x, int pass) {
+    const uint32_t w = (pass & 4) ? uint32_t(x >> 32) : uint32_t(x);
+    return __byte_perm(w, 0u, 0x4440u | uint32_t(pass & 3));
+}
+__device__ __forceinline__ uint32_t digit_of(u128 x, int pass) {
+    const uint64_t h = (pass & 8) ? uint64_t(x >> 64) : uint64_t(x);
+    const uint32_t w = (pass & 4) ? uint32_t(h >> 32) : uint32_t(h);
+    return __byte_perm(w, 0u, 0x4440u | uint32_t(pass & 3));
+}
+
+// ---------------------------------------------------------------------------
+// Status words of the decoupled lookback: [state:2 | epoch:E | value:VB_].
+// state 0 = not published, 1 = PARTIAL (tile-local count), 2 = GLOBAL
+// (inclusive prefix).  The epoch is the digit pass, so one clear per sort
+// serves every pass.  E = log2(key bytes) bits (one per pass value).
+// ---------------------------------------------------------------------------
+template <class W, int KB>
+struct StatusCodec {
+    static constexpr int BITS = 8 * sizeof(W);
+    static constexpr int EPOCH_BITS = KB == 1 ? 0 : KB == 2 ? 1 : KB == 4 ? 2 : KB == 8 ? 3 : 4;
+    static constexpr int VALUE_BITS = BITS - 2 - EPOCH_BITS;
+    static constexpr W VALUE_MASK = (W(1) << VALUE_BITS) - 1;
+    static constexpr W PARTIAL = W(1) << (BITS - 2);
+    static constexpr W GLOBAL = W(2) << (BITS - 2);
+
+    __device__ __forceinline__ static W pack(W state, uint32_t epoch, uint64_t value) {
+        return state | (W(epoch) << VALUE_BITS) | (W(value) & VALUE_MASK);
+    }
+    __device__ __forceinline__ static bool ready(W w, uint32_t epoch) {
+        return (w >> (BITS - 2)) != 0 && uint32_t((w >> VALUE_BITS) & ((W(1) << EPOCH_BITS) - 1)) == epoch;
+    }
+    __device__ __forceinline__ static bool is_global(W w) { return (w & GLOBAL) != 0; }
+    __device__ __forceinline__ static uint64_t value(W w) { return uint64_t(w & VALUE_MASK); }
+};
+
+// ---------------------------------------------------------------------------
+// Memory-order helpers (relaxed, device scope: the value travels in the word).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier + bulk-copy (TMA, non-tensor) helpers.  Plain global->shared bulk
+// copies; no multicast.  Addresses and sizes are 16-byte aligned by callers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                              uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase.  Returns false (after flagging the
+// workspace error word) if the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns,
+                                                  uint32_t* err) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (global_timer_ns() - t0 > limit_ns) {
+            atomicOr(err, ERRBIT_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+// Bounded wait for a status word of the current epoch.  On timeout, or when
+// another CTA already flagged an error, returns a GLOBAL word with value 0 so
+// the lookback walk ends and the launch drains instead of hanging.
+template <class Codec, class W>
+__device__ __forceinline__ W wait_status(const W* addr, uint32_t epoch, uint64_t limit_ns, uint32_t* err) {
+    W w = ld_relaxed(addr);
+    if (Codec::ready(w, epoch)) return w;
+    const uint64_t t0 = global_timer_ns();
+    uint32_t sleep_ns = 32;
+    for (;;) {
+        __nanosleep(sleep_ns);
+        if (sleep_ns < 512) sleep_ns <<= 1;
+        w = ld_relaxed(addr);
+        if (Codec::ready(w, epoch)) return w;
+        if (ld_relaxed(err) != 0u) return Codec::GLOBAL;
+        if (global_timer_ns() - t0 > limit_ns) {
+            atomicOr(err, ERRBIT_TIMEOUT);
+            return Codec::GLOBAL;
+        }
+    }
+}
+
+// Exclusive scan of one value per thread over threads [0, 256) of the block.
+// All threads of the block must call it (it contains __syncthreads).
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan_256(T x, T* warp_tmp /* >= 8 */, T* total_out) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T v = (tid < 256) ? x : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31 && warp < 8) warp_tmp[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        T t = (lane < 8) ? warp_tmp[lane] : T(0);
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            T y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < 8) warp_tmp[lane] = t;  // inclusive warp totals
+    }
+    __syncthreads();
+    T excl = T(0);
+    if (tid < 256) excl = (warp > 0 ? warp_tmp[warp - 1] : T(0)) + v - x;
+    if (total_out) *total_out = warp_tmp[7];
+    return excl;
+}
+
+}  // namespace gbsort

@@ -1,0 +1,392 @@
+// onesweep.cuh — the hot path: global-histogram upsweep and the persistent
+// onesweep digit-binning pass, written for sm_103a (GB300).
+//
+// Reference behaviour followed (AwardOfSky/CUDA-Fast-Sort "rsort" v0.4.0):
+//   upsweep      include/rsort/detail/histogram.cuh:88-211 (all digit
+//                histograms from one read of the keys)
+//   pass kernel  include/rsort/detail/radix_kernel.cuh:118-294 (load +
+//                twiddle, rank, lookback, staged scatter), ranker.cuh:61-170
+//                (warp histograms, early PARTIAL publication, per-item rank by
+//                warp match + popc + leader atomic), lookback.cuh:252-303
+//                (per-bin chained lookback), scatter.cuh:159-202 (stage at
+//                rank in shared memory, thread-linear coalesced write-out)
+// What is GB300-specific here rather than a translation:
+//   - persistent CTAs (grid = SMs x resident CTAs) pull tile ids from a
+//     per-pass atomic counter and double-buffer tiles: while tile t is ranked
+//     and scattered, tile t+1 is already streaming into shared memory by a
+//     bulk copy (cp.async.bulk + mbarrier, L2 evict-first);
+//   - keys stay twiddled between passes (twiddle on the first load and last
+//     store only);
+//   - rank via __match_any_sync (one MATCH per 32 items) instead of 8 ballots;
+//   - status words carry the pass as epoch, so one clear (fused into the
+//     upsweep) serves every pass; all waits are bounded by %globaltimer.
+#pragma once
+
+#include "device_common.cuh"
+#include "shapes.h"
+#include "sort_params.h"
+
+namespace gbsort {
+
+template <int KB>
+struct HistGeom {
+    static constexpr int P = KB;
+    static constexpr int COPIES = P <= 4 ? 32 : (P == 8 ? 16 : 8);
+    static constexpr int NBINS = P * 256;
+    static constexpr size_t SMEM_BYTES = size_t(NBINS) * COPIES * 4;
+};
+
+// Grid-stride copy of `bytes` bytes (16-byte vectors when both sides allow).
+__device__ __forceinline__ void grid_copy(void* dst, const void* src, uint64_t bytes) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const uint64_t t0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+        const uint64_t nv = bytes >> 4;
+        const uint4* s = static_cast<const uint4*>(src);
+        uint4* d = static_cast<uint4*>(dst);
+        for (uint64_t i = t0; i < nv; i += stride) d[i] = s[i];
+        for (uint64_t i = (nv << 4) + t0; i < bytes; i += stride)
+            static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
+    } else {
+        for (uint64_t i = t0; i < bytes; i += stride)
+            static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Upsweep: every digit histogram from one read of the keys.  Counters are
+// spread over COPIES lane-private copies ([bin][copy] layout) so the shared
+// atomics of a warp land in distinct banks; 16-byte vector loads.
+// ---------------------------------------------------------------------------
+template <int KB>
+__global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) {
+    using U = typename KeyBits<KB>::U;
+    using G = HistGeom<KB>;
+    extern __shared__ __align__(16) uint32_t cnt[];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int copy = lane & (G::COPIES - 1);
+
+    for (int i = tid; i < G::NBINS * G::COPIES / 4; i += HIST_THREADS)
+        reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
+
+    // Fused clears / copies that must precede the first pass.
+    {
+        const uint64_t nv = p.status_bytes >> 4;
+        uint4* s = static_cast<uint4*>(p.status);
+        const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+        for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + tid; i < nv; i += stride) s[i] = make_uint4(0, 0, 0, 0);
+        if (p.mirror_keys) grid_copy(p.mirror_keys, p.keys, p.n * KB);
+        if (p.mirror_vals) grid_copy(p.mirror_vals, p.vals, p.val_bytes_total);
+    }
+    __syncthreads();
+
+    const int kind = p.kind, desc = p.desc;
+    auto count = [&](U k) {
+        const U t = twiddle_in<U>(k, kind, desc);
+#pragma unroll
+        for (int d = 0; d < G::P; ++d)
+            atomicAdd(&cnt[(d * 256 + digit_of(t, d)) * G::COPIES + copy], 1u);
+    };
+
+    const U* keys = static_cast<const U*>(p.keys);
+    const uint64_t n = p.n;
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(keys);
+    uint64_t head = ((16u - (addr & 15u)) & 15u) / KB;
+    if (head > n) head = n;
+    const uint64_t nvec = (n - head) * KB / 16;
+    constexpr int PER_VEC = 16 / KB;
+    const uint64_t gthreads = uint64_t(gridDim.x) * HIST_THREADS;
+    const uint64_t gtid = uint64_t(blockIdx.x) * HIST_THREADS + tid;
+
+    if (gtid < head) count(keys[gtid]);
+    const uint4* vec = reinterpret_cast<const uint4*>(keys + head);
+    constexpr int UNROLL = 4;
+    uint64_t i = gtid;
+    for (; i + (UNROLL - 1) * gthreads < nvec; i += UNROLL * gthreads) {
+        uint4 v[UNROLL];
+#pragma unroll
+        for (int r = 0; r < UNROLL; ++r) v[r] = __ldcs(vec + i + r * gthreads);
+#pragma unroll
+        for (int r = 0; r < UNROLL; ++r) {
+            union { uint4 q; U k[PER_VEC]; } w;
+            w.q = v[r];
+#pragma unroll
+            for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
+        }
+    }
+    for (; i < nvec; i += gthreads) {
+        union { uint4 q; U k[PER_VEC]; } w;
+        w.q = __ldcs(vec + i);
+#pragma unroll
+        for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
+    }
+    for (uint64_t j = head + nvec * PER_VEC + gtid; j < n; j += gthreads) count(keys[j]);
+    __syncthreads();
+
+    // Reduce the copies: one warp per bin, conflict-free row read.
+    for (int bin = warp; bin < G::NBINS; bin += HIST_THREADS / 32) {
+        uint32_t s = (lane < G::COPIES) ? cnt[bin * G::COPIES + lane] : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && s) atomicAdd(&p.gp_counts[bin], static_cast<unsigned long long>(s));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Onesweep pass geometry and shared-memory layout.
+// ---------------------------------------------------------------------------
+template <int KB, int VB, int THREADS, int IPT>
+struct PassGeom {
+    static constexpr int WARPS = THREADS / 32;
+    static constexpr int TILE = THREADS * IPT;
+    static constexpr int IPW = 32 * IPT;
+    static constexpr size_t KEY_BYTES = size_t(TILE) * KB;
+    static constexpr size_t VAL_OFF = (KEY_BYTES + 127) & ~size_t(127);
+    static constexpr size_t BUF_BYTES = (VAL_OFF + size_t(TILE) * VB + 127) & ~size_t(127);
+    static constexpr size_t HIST_OFF = 2 * BUF_BYTES;             // u32 [WARPS][256]
+    static constexpr size_t GEXCL_OFF = HIST_OFF + size_t(WARPS) * 256 * 4;  // u64 [256]
+    static constexpr size_t BINB_OFF = GEXCL_OFF + 256 * 8;       // u64 [256]
+    static constexpr size_t SCAN64_OFF = BINB_OFF + 256 * 8;      // u64 [8]
+    static constexpr size_t SCAN32_OFF = SCAN64_OFF + 64;         // u32 [8]
+    static constexpr size_t MBAR_OFF = SCAN32_OFF + 64;           // u64 [2]
+    static constexpr size_t TILEID_OFF = MBAR_OFF + 16;           // u32 [2]
+    static constexpr size_t SMEM_BYTES = TILEID_OFF + 16;
+    static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
+    static_assert(TILE % 16 == 0, "tile starts must stay 16-byte aligned");
+};
+
+template <int KB, int VB, class W, int THREADS, int IPT>
+__global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep_pass_kernel(PassParams p) {
+    using U = typename KeyBits<KB>::U;
+    using V = typename ValBits<VB>::V;
+    using G = PassGeom<KB, VB, THREADS, IPT>;
+    using Codec = StatusCodec<W, KB>;
+    constexpr bool PAIRS = VB > 0;
+
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint32_t* whist = reinterpret_cast<uint32_t*>(smem + G::HIST_OFF);
+    unsigned long long* gexcl = reinterpret_cast<unsigned long long*>(smem + G::GEXCL_OFF);
+    unsigned long long* binb = reinterpret_cast<unsigned long long*>(smem + G::BINB_OFF);
+    unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(smem + G::SCAN64_OFF);
+    uint32_t* scan32 = reinterpret_cast<uint32_t*>(smem + G::SCAN32_OFF);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + G::MBAR_OFF);
+    volatile uint32_t* tile_slot = reinterpret_cast<volatile uint32_t*>(smem + G::TILEID_OFF);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t T = p.num_tiles;
+    const uint64_t n = p.n;
+    const int pass = p.pass, kind = p.kind, desc = p.desc;
+    const uint32_t epoch = uint32_t(pass);
+    W* status = static_cast<W*>(p.status);
+    const U* gkeys_in = static_cast<const U*>(p.keys_in);
+    const V* gvals_in = static_cast<const V*>(p.vals_in);
+
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_mbar_init();
+    }
+    {   // global exclusive digit offsets of this pass (once per CTA)
+        const unsigned long long c = (tid < 256) ? p.gp_counts[tid] : 0ull;
+        const unsigned long long ex = block_exclusive_scan_256<unsigned long long>(c, scan64, nullptr);
+        if (tid < 256) gexcl[tid] = ex;
+    }
+
+    // Thread 0 issues the bulk copies of a tile into buffer `slot`.
+    auto issue_tile = [&](uint32_t t, int slot) {
+        const uint64_t base = uint64_t(t) * G::TILE;
+        const uint64_t rem = n - base;
+        const uint32_t cnt = rem < uint64_t(G::TILE) ? uint32_t(rem) : uint32_t(G::TILE);
+        const uint32_t kb = p.tma_keys ? ((cnt * KB) & ~15u) : 0u;
+        const uint32_t vb = (PAIRS && p.tma_vals) ? ((cnt * VB) & ~15u) : 0u;
+        uint8_t* buf = smem + size_t(slot) * G::BUF_BYTES;
+        mbar_arrive_expect_tx(&mbar[slot], kb + vb);
+        const uint64_t pol = l2_evict_first_policy();
+        if (kb) bulk_copy_g2s(buf, gkeys_in + base, kb, &mbar[slot], pol);
+        if (PAIRS && vb) bulk_copy_g2s(buf + G::VAL_OFF, gvals_in + base, vb, &mbar[slot], pol);
+    };
+
+    __syncthreads();
+    if (tid == 0) {
+        const uint32_t t = atomicAdd(p.tile_counter, 1u);
+        tile_slot[0] = t;
+        if (t < T) issue_tile(t, 0);
+    }
+    __syncthreads();
+    uint32_t cur = tile_slot[0];
+    uint32_t parity = 0;  // bit s: parity of the next wait on buffer s
+    uint32_t it = 0;
+
+    bool next_issued = false;  // thread 0 only: a copy into the other buffer is in flight
+    while (cur < T) {
+        const int b = int(it & 1u);
+        if (tid == 0) {
+            const uint32_t nt = atomicAdd(p.tile_counter, 1u);
+            tile_slot[(it + 1) & 1u] = nt;
+            next_issued = nt < T;
+            if (next_issued) {
+                fence_proxy_async_smem();
+                issue_tile(nt, b ^ 1);
+            }
+        }
+        const bool landed = mbar_wait_bounded(&mbar[b], (parity >> b) & 1u, p.wait_limit_ns, p.err);
+        parity ^= (1u << b);
+
+        const uint64_t tile_base = uint64_t(cur) * G::TILE;
+        const uint64_t rem = n - tile_base;
+        const uint32_t cnt = rem < uint64_t(G::TILE) ? uint32_t(rem) : uint32_t(G::TILE);
+        const bool full = cnt == uint32_t(G::TILE);
+        uint8_t* buf = smem + size_t(b) * G::BUF_BYTES;
+        U* sk = reinterpret_cast<U*>(buf);
+        V* sv = reinterpret_cast<V*>(buf + G::VAL_OFF);
+
+        // ---- load the tile into registers (warp-striped: stable rank order)
+        U keys[IPT];
+        V vals[PAIRS ? IPT : 1];
+        const bool fast = full && p.tma_keys && (!PAIRS || p.tma_vals);
+        if (fast) {
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) {
+                const int j = warp * G::IPW + u * 32 + lane;
+                keys[u] = sk[j];
+                if constexpr (PAIRS) vals[u] = sv[j];
+            }
+        } else {
+            const uint32_t kb = p.tma_keys ? ((cnt * KB) & ~15u) : 0u;
+            const uint32_t vb = p.tma_vals ? ((cnt * VB) & ~15u) : 0u;
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) {
+                const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
+                if (j < cnt) {
+                    keys[u] = ((j + 1) * KB <= kb) ? sk[j] : gkeys_in[tile_base + j];
+                    if constexpr (PAIRS) vals[u] = ((j + 1) * VB <= vb) ? sv[j] : gvals_in[tile_base + j];
+                } else {
+                    keys[u] = U(~U(0));  // tail filler: sorts after every valid key
+                }
+            }
+        }
+        if (p.twiddle_load) {
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) {
+                const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
+                if (full || j < cnt) keys[u] = twiddle_in<U>(keys[u], kind, desc);
+            }
+        }
+
+        // ---- warp-private digit histograms (early counts)
+        uint32_t* wh = whist + warp * 256;
+#pragma unroll
+        for (int i = lane; i < 256; i += 32) wh[i] = 0u;
+        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) atomicAdd(&wh[digit_of(keys[u], pass)], 1u);
+        if (__syncthreads_or(!landed)) {
+            // A bulk copy did not land within the limit (error word already
+            // set).  Publish nothing computed from this buffer — garbage counts
+            // could steer successors' writes — drain the copies still in
+            // flight (bounded) and leave; successors' lookback waits run out
+            // and the launch completes with the error reported.
+            if (tid == 0) {
+                mbar_wait_bounded(&mbar[b], ((parity >> b) & 1u) ^ 1u, DRAIN_LIMIT_NS, p.err);
+                if (next_issued) mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
+            }
+            return;
+        }
+        const uint32_t next_tile = tile_slot[(it + 1) & 1u];
+
+        // ---- per-bin tile totals, warp bases, early PARTIAL publication
+        uint32_t total = 0, valid_total = 0;
+        if (tid < 256) {
+#pragma unroll
+            for (int w = 0; w < G::WARPS; ++w) {
+                const uint32_t c = whist[w * 256 + tid];
+                whist[w * 256 + tid] = total;
+                total += c;
+            }
+            valid_total = total - ((tid == 255) ? (uint32_t(G::TILE) - cnt) : 0u);
+            st_relaxed(status + size_t(cur) * 256 + tid,
+                       Codec::pack(cur == 0 ? Codec::GLOBAL : Codec::PARTIAL, epoch, valid_total));
+        }
+        const uint32_t excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
+        if (tid < 256) {
+#pragma unroll
+            for (int w = 0; w < G::WARPS; ++w) whist[w * 256 + tid] += excl;
+        }
+        __syncthreads();
+
+        // ---- rank: warp match + popc + one shared atomic per digit group
+        uint32_t rank[IPT];
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            const uint32_t d = digit_of(keys[u], pass);
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t below = __popc(peers & lt);
+            uint32_t off = 0;
+            if (below == 0) off = atomicAdd(&wh[d], uint32_t(__popc(peers)));
+            off = __shfl_sync(0xffffffffu, off, __ffs(peers) - 1);
+            rank[u] = off + below;
+        }
+
+        // ---- decoupled lookback (bin owners), GLOBAL publication, bases
+        if (tid < 256) {
+            unsigned long long prefix = 0;
+            if (cur > 0) {
+                uint32_t j = cur - 1;
+                const W* sp = status + size_t(j) * 256 + tid;
+                for (;;) {
+                    const W w = wait_status<Codec>(sp, epoch, p.wait_limit_ns, p.err);
+                    prefix += Codec::value(w);
+                    if (Codec::is_global(w) || j == 0) break;
+                    --j;
+                    sp -= 256;
+                }
+                if (cur + 1 < T)
+                    st_relaxed(status + size_t(cur) * 256 + tid,
+                               Codec::pack(Codec::GLOBAL, epoch, prefix + valid_total));
+            }
+            binb[tid] = gexcl[tid] + prefix - excl;
+        }
+        __syncthreads();
+
+        // ---- stage at rank (this buffer's input is already in registers)
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+#if GBSORT_BOUNDS_CHECK
+            if (rank[u] >= uint32_t(G::TILE)) {
+                atomicOr(p.err, ERRBIT_BOUNDS);
+                continue;
+            }
+#endif
+            sk[rank[u]] = keys[u];
+            if constexpr (PAIRS) sv[rank[u]] = vals[u];
+        }
+        __syncthreads();
+
+        // ---- coalesced write-out: thread-linear over the digit-sorted tile
+        U* okeys = static_cast<U*>(p.keys_out);
+        V* ovals = static_cast<V*>(p.vals_out);
+        const int tw_store = p.twiddle_store;
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            const uint32_t i = uint32_t(u * THREADS + tid);
+            if (full || i < cnt) {
+                const U k = sk[i];
+                const unsigned long long pos = binb[digit_of(k, pass)] + i;
+#if GBSORT_BOUNDS_CHECK
+                if (pos >= n) {
+                    atomicOr(p.err, ERRBIT_BOUNDS);
+                    continue;
+                }
+#endif
+                okeys[pos] = tw_store ? twiddle_out<U>(k, kind, desc) : k;
+                if constexpr (PAIRS) ovals[pos] = sv[i];
+            }
+        }
+        __syncthreads();
+        cur = next_tile;
+        ++it;
+    }
+}
+
+}  // namespace gbsort

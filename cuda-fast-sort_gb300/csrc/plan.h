@@ -1,0 +1,71 @@
+// plan.h — host-side planning of one sort: geometry, workspace layout and
+// launch sizes.  Shared by the plain sort (sort_api.cu) and the batched path.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "shapes.h"
+
+namespace gbsort {
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Control block at the start of the workspace's control region:
+//   [gp_counts: passes*256 u64][tile_counters: 16 u32][err: u32][pad]
+struct CtlLayout {
+    size_t gp_off = 0;
+    size_t counters_off = 0;
+    size_t err_off = 0;
+    size_t bytes = 0;
+    static CtlLayout make(int passes) {
+        CtlLayout c;
+        c.gp_off = 0;
+        c.counters_off = size_t(passes) * 256 * 8;
+        c.err_off = c.counters_off + 16 * 4;
+        c.bytes = align_up(c.err_off + 4, 256);
+        return c;
+    }
+};
+
+struct Plan {
+    int key_type = 0;
+    int kb = 0;            // key bytes
+    int vb = 0;            // value bytes (0: keys only)
+    int kind = 0;          // KeyKind
+    int passes = 0;
+    bool wide_status = false;
+    KernelEntry pass{};
+    KernelEntry upsweep{};
+    uint64_t n = 0;
+    uint32_t num_tiles = 0;
+    // workspace layout (offsets from the workspace base)
+    size_t alt_keys_off = 0;
+    size_t alt_vals_off = 0;
+    size_t ctl_off = 0;
+    size_t status_off = 0;
+    size_t status_bytes = 0;
+    size_t total_bytes = 0;
+    CtlLayout ctl{};
+};
+
+// Fills *plan; returns a gbsort_status code.
+int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan);
+
+// Enqueues one sort on `stream`.  `ms` (optional) receives per-kernel event
+// times after a stream sync: [upsweep, pass 0 .. pass P-1].
+int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values, void* d_workspace,
+                 cudaStream_t stream, float* ms, int ms_cap, int* n_ms);
+
+// Device facts (cached per device).
+int device_sm_count();
+int device_is_sm103();
+int resident_ctas(const KernelEntry& e);  // per SM, after opting in to the smem
+int prepare_kernel(const KernelEntry& e); // cudaFuncSetAttribute once per device
+
+uint64_t wait_limit_ns();
+void set_last_error(const char* what, cudaError_t err);
+
+}  // namespace gbsort

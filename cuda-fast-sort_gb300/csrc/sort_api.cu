@@ -1,0 +1,538 @@
+// sort_api.cu — C ABI of the plain sort (include/gbsort.h) and its host
+// planning / enqueue logic.
+//
+// Reference host path replaced (AwardOfSky/CUDA-Fast-Sort "rsort" v0.4.0):
+//   include/rsort/rsort.cuh:13-92                 public templates
+//   include/rsort/detail/radix_kernel.cuh:35-109  workspace build/bind
+//   include/rsort/detail/radix_kernel.cuh:336-474 enqueue: memsets, histogram
+//                                                 launch, pass loop, ping-pong
+//   include/rsort/detail/radix_kernel.cuh:486-607 size query, policy switch,
+//                                                 per-call graph wrapper
+// Per sort this enqueues one small memset (digit counts, tile counters,
+// error word), one upsweep launch and one persistent launch per digit pass,
+// all on the caller's stream; nothing is allocated and nothing synchronizes.
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "gbsort.h"
+#include "plan.h"
+#include "device_common.cuh"
+#include "sort_params.h"
+
+namespace gbsort {
+
+const KernelEntry* pass_entries_k1();
+const KernelEntry* pass_entries_k2();
+const KernelEntry* pass_entries_k4();
+const KernelEntry* pass_entries_k8();
+const KernelEntry* pass_entries_k16();
+const KernelEntry* upsweep_entry_k1();
+const KernelEntry* upsweep_entry_k2();
+const KernelEntry* upsweep_entry_k4();
+const KernelEntry* upsweep_entry_k8();
+const KernelEntry* upsweep_entry_k16();
+
+const KernelEntry* pass_entries(int kb) {
+    switch (kb) {
+        case 1: return pass_entries_k1();
+        case 2: return pass_entries_k2();
+        case 4: return pass_entries_k4();
+        case 8: return pass_entries_k8();
+        case 16: return pass_entries_k16();
+        default: return nullptr;
+    }
+}
+
+const KernelEntry* upsweep_entry(int kb) {
+    switch (kb) {
+        case 1: return upsweep_entry_k1();
+        case 2: return upsweep_entry_k2();
+        case 4: return upsweep_entry_k4();
+        case 8: return upsweep_entry_k8();
+        case 16: return upsweep_entry_k16();
+        default: return nullptr;
+    }
+}
+
+namespace {
+
+std::atomic<uint64_t> g_wait_limit_ns{2000000000ull};
+thread_local std::string g_last_error;
+
+constexpr int MAX_DEVICES = 64;
+
+struct DeviceFacts {
+    std::once_flag once;
+    int sms = 0;
+    int cc = 0;
+};
+DeviceFacts g_dev[MAX_DEVICES];
+
+int current_device() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= MAX_DEVICES) return -1;
+    return d;
+}
+
+DeviceFacts* facts() {
+    const int d = current_device();
+    if (d < 0) return nullptr;
+    DeviceFacts* f = &g_dev[d];
+    std::call_once(f->once, [f, d] {
+        int sms = 0, ma = 0, mi = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+        cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, d);
+        cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, d);
+        f->sms = sms;
+        f->cc = ma * 10 + mi;
+    });
+    return f;
+}
+
+// Per (device, kernel) opt-in to large dynamic shared memory + occupancy.
+struct KernelPrep {
+    const void* fn = nullptr;
+    int device = -1;
+    int occ = 0;
+    int status = -1;
+};
+std::mutex g_prep_mu;
+KernelPrep g_prep[512];
+
+KernelPrep* prep_for(const KernelEntry& e) {
+    const int d = current_device();
+    if (d < 0) return nullptr;
+    std::lock_guard<std::mutex> lk(g_prep_mu);
+    for (auto& p : g_prep) {
+        if (p.fn == e.fn && p.device == d) return &p;
+    }
+    for (auto& p : g_prep) {
+        if (p.fn == nullptr) {
+            p.fn = e.fn;
+            p.device = d;
+            cudaError_t err = cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(e.smem));
+            if (err == cudaSuccess)
+                err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p.occ, e.fn, e.threads, e.smem);
+            if (err != cudaSuccess) {
+                set_last_error("kernel preparation", err);
+                p.status = GBSORT_ERR_CUDA;
+                cudaGetLastError();
+            } else {
+                p.status = p.occ > 0 ? GBSORT_OK : GBSORT_ERR_UNSUPPORTED;
+            }
+            return &p;
+        }
+    }
+    return nullptr;
+}
+
+int key_kind_of(int kt) {
+    if (kt >= GBSORT_KEY_F32) return KIND_FLOAT;
+    if (kt >= GBSORT_KEY_I8) return KIND_SIGNED;
+    return KIND_UNSIGNED;
+}
+
+int log2_exact(int x) {
+    int r = 0;
+    while ((1 << r) < x) ++r;
+    return r;
+}
+
+}  // namespace
+
+uint64_t wait_limit_ns() { return g_wait_limit_ns.load(std::memory_order_relaxed); }
+
+void set_last_error(const char* what, cudaError_t err) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(err);
+}
+
+int device_sm_count() {
+    DeviceFacts* f = facts();
+    return f ? f->sms : 0;
+}
+
+int device_is_sm103() {
+    DeviceFacts* f = facts();
+    return f && f->cc == 103;
+}
+
+int prepare_kernel(const KernelEntry& e) {
+    KernelPrep* p = prep_for(e);
+    return p ? p->status : GBSORT_ERR_CUDA;
+}
+
+int resident_ctas(const KernelEntry& e) {
+    KernelPrep* p = prep_for(e);
+    return p ? p->occ : 0;
+}
+
+int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    const int vi = value_index(int(value_bytes));
+    if (kb == 0 || vi < 0 || value_bytes > 16) return GBSORT_ERR_INVALID_ARGUMENT;
+    Plan p;
+    p.key_type = key_type;
+    p.kb = int(kb);
+    p.vb = int(value_bytes);
+    p.kind = key_kind_of(key_type);
+    p.passes = int(kb);
+    p.n = n;
+    // 32-bit status words hold values < 2^(30 - log2(passes)); every published
+    // value is < n (the last tile never publishes an inclusive prefix).
+    const int value_bits32 = 30 - log2_exact(p.passes);
+    p.wide_status = n > (uint64_t(1) << value_bits32);
+    p.pass = pass_entries(p.kb)[vi * 2 + (p.wide_status ? 1 : 0)];
+    p.upsweep = *upsweep_entry(p.kb);
+    const uint64_t tiles = (n + uint64_t(p.pass.tile) - 1) / uint64_t(p.pass.tile);
+    if (tiles > 0xFFFFFFFFull) return GBSORT_ERR_INVALID_ARGUMENT;
+    p.num_tiles = uint32_t(tiles);
+    size_t off = 0;
+    p.alt_keys_off = off;
+    off = align_up(off + size_t(n) * kb, 256);
+    p.alt_vals_off = off;
+    off = align_up(off + size_t(n) * value_bytes, 256);
+    p.ctl = CtlLayout::make(p.passes);
+    p.ctl_off = off;
+    off = align_up(off + p.ctl.bytes, 256);
+    p.status_off = off;
+    p.status_bytes = size_t(p.num_tiles) * 256 * (p.wide_status ? 8 : 4);
+    off = align_up(off + p.status_bytes, 256);
+    p.total_bytes = off;
+    *plan = p;
+    return GBSORT_OK;
+}
+
+int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values, void* d_workspace,
+                 cudaStream_t stream, float* ms, int ms_cap, int* n_ms) {
+    if (n_ms) *n_ms = 0;
+    if (plan.n == 0) return GBSORT_OK;
+    if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
+    int st = prepare_kernel(plan.pass);
+    if (st != GBSORT_OK) return st;
+    st = prepare_kernel(plan.upsweep);
+    if (st != GBSORT_OK) return st;
+
+    uint8_t* ws = static_cast<uint8_t*>(d_workspace);
+    uint8_t* ctl = ws + plan.ctl_off;
+    unsigned long long* gp = reinterpret_cast<unsigned long long*>(ctl + plan.ctl.gp_off);
+    uint32_t* counters = reinterpret_cast<uint32_t*>(ctl + plan.ctl.counters_off);
+    uint32_t* err_word = reinterpret_cast<uint32_t*>(ctl + plan.ctl.err_off);
+    void* status = ws + plan.status_off;
+    void* alt_keys = ws + plan.alt_keys_off;
+    void* alt_vals = plan.vb ? ws + plan.alt_vals_off : nullptr;
+    const bool odd = (plan.passes & 1) != 0;
+    const int sms = device_sm_count();
+
+    const int nev = plan.passes + 2;
+    cudaEvent_t ev[20] = {};
+    const bool timed = ms != nullptr;
+    if (timed) {
+        for (int i = 0; i < nev; ++i) {
+            if (cudaEventCreate(&ev[i]) != cudaSuccess) return GBSORT_ERR_CUDA;
+        }
+    }
+    auto fail = [&](const char* what, cudaError_t e) {
+        set_last_error(what, e);
+        if (timed)
+            for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
+        return GBSORT_ERR_CUDA;
+    };
+
+    cudaError_t e = cudaMemsetAsync(ctl, 0, plan.ctl.bytes, stream);
+    if (e != cudaSuccess) return fail("memset control block", e);
+
+    HistParams hp{};
+    hp.keys = d_keys;
+    hp.n = plan.n;
+    hp.kind = plan.kind;
+    hp.desc = descending;
+    hp.gp_counts = gp;
+    hp.status = status;
+    hp.status_bytes = plan.status_bytes;
+    hp.mirror_keys = odd ? alt_keys : nullptr;
+    hp.vals = d_values;
+    hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
+    hp.val_bytes_total = plan.n * uint64_t(plan.vb);
+    const uint64_t hist_work = (plan.n * uint64_t(plan.kb) + (HIST_THREADS * 64ull) - 1) /
+                               (HIST_THREADS * 64ull);
+    uint32_t hist_ctas = uint32_t(hist_work < uint64_t(sms) ? hist_work : uint64_t(sms));
+    if (hist_ctas == 0) hist_ctas = 1;
+    {
+        void* args[] = {&hp};
+        if (timed) cudaEventRecord(ev[0], stream);
+        e = cudaLaunchKernel(plan.upsweep.fn, dim3(hist_ctas), dim3(plan.upsweep.threads), args,
+                             plan.upsweep.smem, stream);
+        if (e != cudaSuccess) return fail("upsweep launch", e);
+        if (timed) cudaEventRecord(ev[1], stream);
+    }
+
+    const int occ = resident_ctas(plan.pass);
+    const uint64_t max_ctas = uint64_t(sms) * uint64_t(occ > 0 ? occ : 1);
+    const uint32_t pass_ctas = uint32_t(plan.num_tiles < max_ctas ? plan.num_tiles : max_ctas);
+    for (int pass = 0; pass < plan.passes; ++pass) {
+        // Even passes read the user's buffer unless the mirror made the
+        // alternate buffer the source (odd pass counts end in place).
+        const bool from_user = ((pass + (odd ? 1 : 0)) & 1) == 0;
+        PassParams pp{};
+        pp.keys_in = from_user ? d_keys : alt_keys;
+        pp.keys_out = from_user ? alt_keys : d_keys;
+        pp.vals_in = plan.vb ? (from_user ? d_values : alt_vals) : nullptr;
+        pp.vals_out = plan.vb ? (from_user ? alt_vals : d_values) : nullptr;
+        pp.n = plan.n;
+        pp.num_tiles = plan.num_tiles;
+        pp.pass = pass;
+        pp.kind = plan.kind;
+        pp.desc = descending;
+        pp.twiddle_load = pass == 0;
+        pp.twiddle_store = pass == plan.passes - 1;
+        pp.tma_keys = (reinterpret_cast<uintptr_t>(pp.keys_in) & 15) == 0;
+        pp.tma_vals = plan.vb ? ((reinterpret_cast<uintptr_t>(pp.vals_in) & 15) == 0) : 0;
+        pp.gp_counts = gp + size_t(pass) * 256;
+        pp.status = status;
+        pp.tile_counter = counters + pass;
+        pp.err = err_word;
+        pp.wait_limit_ns = wait_limit_ns();
+        void* args[] = {&pp};
+        e = cudaLaunchKernel(plan.pass.fn, dim3(pass_ctas), dim3(plan.pass.threads), args, plan.pass.smem, stream);
+        if (e != cudaSuccess) return fail("pass launch", e);
+        if (timed) cudaEventRecord(ev[2 + pass], stream);
+    }
+
+    if (timed) {
+        e = cudaEventSynchronize(ev[nev - 1]);
+        if (e != cudaSuccess) return fail("event sync", e);
+        int w = 0;
+        for (int i = 0; i + 1 < nev && w < ms_cap; ++i) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+            ms[w++] = t;
+        }
+        if (n_ms) *n_ms = w;
+        for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
+    }
+    return GBSORT_OK;
+}
+
+}  // namespace gbsort
+
+using namespace gbsort;
+
+namespace {
+
+int status_from_error_word(uint32_t err) {
+    if (err & ERRBIT_BOUNDS) return GBSORT_ERR_INTERNAL;
+    if (err & ERRBIT_TIMEOUT) return GBSORT_ERR_TIMEOUT;
+    return GBSORT_OK;
+}
+
+int check_args(int key_type, size_t value_bytes, void* d_keys, void* d_values, size_t* temp_bytes) {
+    if (temp_bytes == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (gbsort_key_bytes(key_type) == 0) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (value_index(int(value_bytes)) < 0 || value_bytes > 16) return GBSORT_ERR_INVALID_ARGUMENT;
+    (void)d_keys;
+    (void)d_values;
+    return GBSORT_OK;
+}
+
+int sort_common(int key_type, int descending, void* d_keys, void* d_values, size_t value_bytes,
+                size_t* temp_bytes, void* d_workspace, size_t n, void* stream) {
+    int st = check_args(key_type, value_bytes, d_keys, d_values, temp_bytes);
+    if (st != GBSORT_OK) return st;
+    Plan plan;
+    st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (d_workspace == nullptr) {
+        *temp_bytes = plan.total_bytes;
+        return GBSORT_OK;
+    }
+    if (n == 0) return GBSORT_OK;
+    if (d_keys == nullptr || (value_bytes != 0 && d_values == nullptr)) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (*temp_bytes < plan.total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    return enqueue_sort(plan, descending ? 1 : 0, d_keys, d_values, d_workspace,
+                        static_cast<cudaStream_t>(stream), nullptr, 0, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t gbsort_key_bytes(int key_type) {
+    static const size_t b[GBSORT_KEY_COUNT] = {1, 2, 4, 8, 16, 1, 2, 4, 8, 16, 4, 8, 16};
+    return (key_type >= 0 && key_type < GBSORT_KEY_COUNT) ? b[key_type] : 0;
+}
+
+const char* gbsort_status_string(int status) {
+    switch (status) {
+        case GBSORT_OK: return "ok";
+        case GBSORT_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case GBSORT_ERR_WORKSPACE_TOO_SMALL: return "workspace too small";
+        case GBSORT_ERR_CUDA: return "CUDA error";
+        case GBSORT_ERR_TIMEOUT: return "device wait timed out";
+        case GBSORT_ERR_UNSUPPORTED: return "unsupported device (needs compute capability 10.3)";
+        case GBSORT_ERR_BUDGET: return "request exceeds the memory budget";
+        case GBSORT_ERR_NOT_READY: return "not ready";
+        case GBSORT_ERR_INTERNAL: return "device bounds check fired (internal error)";
+        default: return "unknown status";
+    }
+}
+
+const char* gbsort_version(void) { return "gbsort 1.0 sm_103a onesweep"; }
+
+const char* gbsort_last_error(void) { return g_last_error.c_str(); }
+
+int gbsort_sort_keys(int key_type, int descending, void* d_keys, size_t* temp_bytes, void* d_workspace,
+                     size_t n, void* stream) {
+    return sort_common(key_type, descending, d_keys, nullptr, 0, temp_bytes, d_workspace, n, stream);
+}
+
+int gbsort_sort_pairs(int key_type, int descending, void* d_keys, void* d_values, size_t value_bytes,
+                      size_t* temp_bytes, void* d_workspace, size_t n, void* stream) {
+    return sort_common(key_type, descending, d_keys, d_values, value_bytes, temp_bytes, d_workspace, n, stream);
+}
+
+#define GBSORT_DEFINE_TYPED(name, KT)                                                                     \
+    int gbsort_sort_##name(void* k, size_t* tb, void* ws, size_t n, void* s) {                            \
+        return sort_common(KT, 0, k, nullptr, 0, tb, ws, n, s);                                           \
+    }                                                                                                     \
+    int gbsort_sort_##name##_desc(void* k, size_t* tb, void* ws, size_t n, void* s) {                     \
+        return sort_common(KT, 1, k, nullptr, 0, tb, ws, n, s);                                           \
+    }                                                                                                     \
+    int gbsort_sort_pairs_##name(void* k, void* v, size_t vb, size_t* tb, void* ws, size_t n, void* s) {  \
+        return sort_common(KT, 0, k, v, vb, tb, ws, n, s);                                                \
+    }                                                                                                     \
+    int gbsort_sort_pairs_##name##_desc(void* k, void* v, size_t vb, size_t* tb, void* ws, size_t n,      \
+                                        void* s) {                                                        \
+        return sort_common(KT, 1, k, v, vb, tb, ws, n, s);                                                \
+    }
+GBSORT_DEFINE_TYPED(u8, GBSORT_KEY_U8)
+GBSORT_DEFINE_TYPED(u16, GBSORT_KEY_U16)
+GBSORT_DEFINE_TYPED(u32, GBSORT_KEY_U32)
+GBSORT_DEFINE_TYPED(u64, GBSORT_KEY_U64)
+GBSORT_DEFINE_TYPED(u128, GBSORT_KEY_U128)
+GBSORT_DEFINE_TYPED(i8, GBSORT_KEY_I8)
+GBSORT_DEFINE_TYPED(i16, GBSORT_KEY_I16)
+GBSORT_DEFINE_TYPED(i32, GBSORT_KEY_I32)
+GBSORT_DEFINE_TYPED(i64, GBSORT_KEY_I64)
+GBSORT_DEFINE_TYPED(i128, GBSORT_KEY_I128)
+GBSORT_DEFINE_TYPED(f32, GBSORT_KEY_F32)
+GBSORT_DEFINE_TYPED(f64, GBSORT_KEY_F64)
+GBSORT_DEFINE_TYPED(f128, GBSORT_KEY_F128)
+#undef GBSORT_DEFINE_TYPED
+
+size_t gbsort_host_buffer_bytes(int key_type, size_t value_bytes, size_t n) {
+    Plan plan;
+    if (make_plan(key_type, value_bytes, n, &plan) != GBSORT_OK) return 0;
+    size_t off = align_up(n * size_t(plan.kb), 256);
+    off = align_up(off + n * value_bytes, 256);
+    return off + plan.total_bytes;
+}
+
+int gbsort_sort_host(int key_type, int descending, void* h_keys, void* h_values, size_t value_bytes, size_t n,
+                     void* d_buffer, size_t buffer_bytes, void* stream) {
+    Plan plan;
+    int st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (n == 0) return GBSORT_OK;
+    if (h_keys == nullptr || d_buffer == nullptr || (value_bytes && h_values == nullptr))
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    const size_t need = gbsort_host_buffer_bytes(key_type, value_bytes, n);
+    if (buffer_bytes < need) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint8_t* base = static_cast<uint8_t*>(d_buffer);
+    const size_t kbytes = n * size_t(plan.kb), vbytes = n * value_bytes;
+    uint8_t* d_keys = base;
+    uint8_t* d_vals = base + align_up(kbytes, 256);
+    uint8_t* d_ws = base + align_up(align_up(kbytes, 256) + vbytes, 256);
+    cudaError_t e = cudaMemcpyAsync(d_keys, h_keys, kbytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && vbytes) e = cudaMemcpyAsync(d_vals, h_values, vbytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        set_last_error("host to device copy", e);
+        return GBSORT_ERR_CUDA;
+    }
+    st = enqueue_sort(plan, descending ? 1 : 0, d_keys, value_bytes ? d_vals : nullptr, d_ws, s, nullptr, 0,
+                      nullptr);
+    if (st != GBSORT_OK) return st;
+    e = cudaMemcpyAsync(h_keys, d_keys, kbytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && vbytes) e = cudaMemcpyAsync(h_values, d_vals, vbytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_last_error("device to host copy", e);
+        return GBSORT_ERR_CUDA;
+    }
+    uint32_t err = 0;
+    e = cudaMemcpy(&err, d_ws + plan.ctl_off + plan.ctl.err_off, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return GBSORT_ERR_CUDA;
+    return status_from_error_word(err);
+}
+
+int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {
+    Plan plan;
+    int st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (d_workspace == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (n == 0) return GBSORT_OK;
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        set_last_error("stream sync", e);
+        return GBSORT_ERR_CUDA;
+    }
+    uint32_t err = 0;
+    e = cudaMemcpy(&err, static_cast<uint8_t*>(d_workspace) + plan.ctl_off + plan.ctl.err_off, 4,
+                   cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_last_error("status read", e);
+        return GBSORT_ERR_CUDA;
+    }
+    return status_from_error_word(err);
+}
+
+void gbsort_set_wait_limit_ns(uint64_t ns) { g_wait_limit_ns.store(ns, std::memory_order_relaxed); }
+uint64_t gbsort_get_wait_limit_ns(void) { return wait_limit_ns(); }
+
+int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* out) {
+    if (out == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    Plan plan;
+    int st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    std::memset(out, 0, sizeof(*out));
+    out->passes = uint32_t(plan.passes);
+    out->radix_bits = 8;
+    out->tile_items = uint32_t(plan.pass.tile);
+    out->threads = uint32_t(plan.pass.threads);
+    out->items_per_thread = uint32_t(plan.pass.ipt);
+    out->num_tiles = plan.num_tiles;
+    const int sms = device_sm_count();
+    if (sms > 0 && prepare_kernel(plan.pass) == GBSORT_OK) {
+        const uint64_t max_ctas = uint64_t(sms) * uint64_t(resident_ctas(plan.pass));
+        out->pass_ctas = uint32_t(plan.num_tiles < max_ctas ? plan.num_tiles : max_ctas);
+        out->hist_ctas = uint32_t(sms);
+    }
+    out->status_word_bytes = plan.wide_status ? 8 : 4;
+    out->kernel_launches = uint32_t(plan.passes + 1);
+    out->workspace_bytes = plan.total_bytes;
+    return GBSORT_OK;
+}
+
+int gbsort_sort_timed(int key_type, int descending, void* d_keys, void* d_values, size_t value_bytes,
+                      void* d_workspace, size_t temp_bytes, size_t n, void* stream, float* ms_out, int ms_cap,
+                      int* n_ms) {
+    Plan plan;
+    int st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (n == 0) {
+        if (n_ms) *n_ms = 0;
+        return GBSORT_OK;
+    }
+    if (d_keys == nullptr || d_workspace == nullptr || ms_out == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (temp_bytes < plan.total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    return enqueue_sort(plan, descending ? 1 : 0, d_keys, d_values, d_workspace,
+                        static_cast<cudaStream_t>(stream), ms_out, ms_cap, n_ms);
+}
+
+int gbsort_device_sm_count(void) { return device_sm_count(); }
+
+}  // extern "C"

@@ -1,0 +1,47 @@
+// sort_params.h — launch parameter blocks shared by host and device code.
+#pragma once
+
+#include <cstdint>
+
+namespace gbsort {
+
+// Global-histogram upsweep (one launch per sort).
+struct HistParams {
+    const void* keys;           // user keys (raw bits)
+    uint64_t n;
+    int kind;                   // KeyKind
+    int desc;                   // descending
+    unsigned long long* gp_counts;  // [passes][256] digit counts, zeroed before launch
+    void* status;               // lookback status array to clear
+    uint64_t status_bytes;      // multiple of 16
+    // Odd pass counts (1-byte keys) end in the alternate buffer; the upsweep
+    // then also mirrors keys/values there so the single pass lands in place.
+    void* mirror_keys;          // nullptr: no mirroring
+    const void* vals;
+    void* mirror_vals;
+    uint64_t val_bytes_total;   // n * value bytes
+};
+
+// One onesweep digit pass (one persistent launch per digit).
+struct PassParams {
+    const void* keys_in;
+    void* keys_out;
+    const void* vals_in;
+    void* vals_out;
+    uint64_t n;
+    uint32_t num_tiles;
+    int pass;                   // digit index, 0 = least significant byte
+    int kind;
+    int desc;
+    int twiddle_load;           // first pass: map raw keys to ordered bits
+    int twiddle_store;          // last pass: map ordered bits back to keys
+    int tma_keys;               // keys_in 16-byte aligned: tiles arrive by bulk copy
+    int tma_vals;
+    const unsigned long long* gp_counts;  // this pass's row [256]
+    void* status;               // [num_tiles][256] status words
+    uint32_t* tile_counter;     // this pass's dynamic tile counter (zeroed)
+    uint32_t* err;              // workspace error word
+    uint64_t wait_limit_ns;
+};
+
+}  // namespace gbsort

@@ -1,0 +1,237 @@
+"""ctypes binding of libgbsort.so (the C ABI declared in include/gbsort.h).
+
+This is a thin host-side mirror of rsort's entry points for Python callers
+(tests, benchmark): ``sort`` / ``sort_descending`` / ``sort_pairs`` /
+``sort_pairs_descending`` with rsort's size-query + workspace protocol
+(reference include/rsort/rsort.cuh:13-92).  Device memory is handed in as raw
+pointers (``int``) or as torch tensors (only their ``data_ptr()`` is used).
+
+There is no fallback: if libgbsort.so is missing, importing the binding
+raises ``GbsortUnavailable``; build it with ``python cuda-fast-sort_gb300/build.py``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libgbsort.so")
+
+KEY_TYPES = {
+    "u8": 0, "u16": 1, "u32": 2, "u64": 3, "u128": 4,
+    "i8": 5, "i16": 6, "i32": 7, "i64": 8, "i128": 9,
+    "f32": 10, "f64": 11, "f128": 12,
+}
+KEY_BYTES = {"u8": 1, "u16": 2, "u32": 4, "u64": 8, "u128": 16, "i8": 1, "i16": 2, "i32": 4,
+             "i64": 8, "i128": 16, "f32": 4, "f64": 8, "f128": 16}
+TYPED_NAMES = list(KEY_TYPES)
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_WORKSPACE_TOO_SMALL = 2
+ERR_CUDA = 3
+ERR_TIMEOUT = 4
+ERR_UNSUPPORTED = 5
+ERR_BUDGET = 6
+ERR_NOT_READY = 7
+
+
+class GbsortUnavailable(RuntimeError):
+    pass
+
+
+class GbsortError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = f"{what}: " if what else ""
+        super().__init__(f"{msg}gbsort status {status} ({status_string(status)}) {last_error()}".strip())
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("passes", ctypes.c_uint32), ("radix_bits", ctypes.c_uint32), ("tile_items", ctypes.c_uint32),
+        ("threads", ctypes.c_uint32), ("items_per_thread", ctypes.c_uint32), ("num_tiles", ctypes.c_uint32),
+        ("pass_ctas", ctypes.c_uint32), ("hist_ctas", ctypes.c_uint32), ("status_word_bytes", ctypes.c_uint32),
+        ("kernel_launches", ctypes.c_uint32), ("workspace_bytes", ctypes.c_uint64),
+    ]
+
+
+_lib = None
+
+
+def _declare(lib: ctypes.CDLL) -> None:
+    vp, sz, i, u64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint64
+    psz = ctypes.POINTER(ctypes.c_size_t)
+    sig = {
+        "gbsort_key_bytes": (sz, [i]),
+        "gbsort_status_string": (ctypes.c_char_p, [i]),
+        "gbsort_version": (ctypes.c_char_p, []),
+        "gbsort_last_error": (ctypes.c_char_p, []),
+        "gbsort_sort_keys": (i, [i, i, vp, psz, vp, sz, vp]),
+        "gbsort_sort_pairs": (i, [i, i, vp, vp, sz, psz, vp, sz, vp]),
+        "gbsort_host_buffer_bytes": (sz, [i, sz, sz]),
+        "gbsort_sort_host": (i, [i, i, vp, vp, sz, sz, vp, sz, vp]),
+        "gbsort_workspace_status": (i, [i, sz, sz, vp, vp]),
+        "gbsort_set_wait_limit_ns": (None, [u64]),
+        "gbsort_get_wait_limit_ns": (u64, []),
+        "gbsort_probe_wait_timeout": (i, [vp, u64, vp]),
+        "gbsort_plan": (i, [i, sz, sz, ctypes.POINTER(PlanInfo)]),
+        "gbsort_sort_timed": (i, [i, i, vp, vp, sz, vp, sz, sz, vp, ctypes.POINTER(ctypes.c_float), i,
+                                  ctypes.POINTER(ctypes.c_int)]),
+        "gbsort_generate": (i, [i, sz, vp, sz, u64, vp]),
+        "gbsort_device_sm_count": (i, []),
+    }
+    for name in TYPED_NAMES:
+        sig[f"gbsort_sort_{name}"] = (i, [vp, psz, vp, sz, vp])
+        sig[f"gbsort_sort_{name}_desc"] = (i, [vp, psz, vp, sz, vp])
+        sig[f"gbsort_sort_pairs_{name}"] = (i, [vp, vp, sz, psz, vp, sz, vp])
+        sig[f"gbsort_sort_pairs_{name}_desc"] = (i, [vp, vp, sz, psz, vp, sz, vp])
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libgbsort.so (once); raises GbsortUnavailable if it is not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise GbsortUnavailable(f"{LIB_PATH} is not built (run cuda-fast-sort_gb300/build.py)")
+        l = ctypes.CDLL(LIB_PATH)
+        _declare(l)
+        _lib = l
+    return _lib
+
+
+def status_string(status: int) -> str:
+    return lib().gbsort_status_string(status).decode()
+
+
+def last_error() -> str:
+    return lib().gbsort_last_error().decode()
+
+
+def _ptr(x) -> int | None:
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return int(x.data_ptr())
+
+
+def _stream(s) -> int | None:
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return int(s.cuda_stream)
+
+
+def _check(status: int, what: str) -> None:
+    if status != OK:
+        raise GbsortError(status, what)
+
+
+def key_type_id(key_type) -> int:
+    return KEY_TYPES[key_type] if isinstance(key_type, str) else int(key_type)
+
+
+def temp_bytes(key_type, n: int, value_bytes: int = 0) -> int:
+    """rsort's size query: workspace bytes for (key type, value size, n)."""
+    tb = ctypes.c_size_t(0)
+    kt = key_type_id(key_type)
+    if value_bytes:
+        st = lib().gbsort_sort_pairs(kt, 0, None, None, value_bytes, ctypes.byref(tb), None, n, None)
+    else:
+        st = lib().gbsort_sort_keys(kt, 0, None, ctypes.byref(tb), None, n, None)
+    _check(st, "size query")
+    return tb.value
+
+
+def sort(keys, n: int, key_type, workspace, workspace_bytes: int, *, values=None, value_bytes: int = 0,
+         descending: bool = False, stream=None) -> None:
+    """In-place device sort (keys-only if values is None).  Raises GbsortError."""
+    kt = key_type_id(key_type)
+    tb = ctypes.c_size_t(workspace_bytes)
+    if values is None:
+        st = lib().gbsort_sort_keys(kt, int(descending), _ptr(keys), ctypes.byref(tb), _ptr(workspace), n,
+                                    _stream(stream))
+    else:
+        st = lib().gbsort_sort_pairs(kt, int(descending), _ptr(keys), _ptr(values), value_bytes, ctypes.byref(tb),
+                                     _ptr(workspace), n, _stream(stream))
+    _check(st, "sort")
+
+
+def sort_timed(keys, n: int, key_type, workspace, workspace_bytes: int, *, values=None, value_bytes: int = 0,
+               descending: bool = False, stream=None) -> list[float]:
+    """Sort with a CUDA event around every kernel; returns per-kernel ms
+    ([upsweep, pass 0, ..., pass P-1]).  Synchronizes the stream."""
+    kt = key_type_id(key_type)
+    ms = (ctypes.c_float * 32)()
+    cnt = ctypes.c_int(0)
+    st = lib().gbsort_sort_timed(kt, int(descending), _ptr(keys), _ptr(values), value_bytes if values is not None
+                                 else 0, _ptr(workspace), workspace_bytes, n, _stream(stream), ms, 32,
+                                 ctypes.byref(cnt))
+    _check(st, "timed sort")
+    return [ms[i] for i in range(cnt.value)]
+
+
+def workspace_status(key_type, n: int, workspace, value_bytes: int = 0, stream=None) -> int:
+    return lib().gbsort_workspace_status(key_type_id(key_type), value_bytes, n, _ptr(workspace), _stream(stream))
+
+
+@dataclass
+class Plan:
+    passes: int
+    radix_bits: int
+    tile_items: int
+    threads: int
+    items_per_thread: int
+    num_tiles: int
+    pass_ctas: int
+    hist_ctas: int
+    status_word_bytes: int
+    kernel_launches: int
+    workspace_bytes: int
+
+
+def plan(key_type, n: int, value_bytes: int = 0) -> Plan:
+    info = PlanInfo()
+    _check(lib().gbsort_plan(key_type_id(key_type), value_bytes, n, ctypes.byref(info)), "plan")
+    return Plan(*(getattr(info, f) for f, _ in PlanInfo._fields_))
+
+
+def generate(dist: int, key_bytes: int, out, n: int, seed: int, stream=None) -> None:
+    _check(lib().gbsort_generate(dist, key_bytes, _ptr(out), n, seed, _stream(stream)), "generate")
+
+
+def host_buffer_bytes(key_type, n: int, value_bytes: int = 0) -> int:
+    return lib().gbsort_host_buffer_bytes(key_type_id(key_type), value_bytes, n)
+
+
+def sort_host(h_keys, n: int, key_type, d_buffer, buffer_bytes: int, *, h_values=None, value_bytes: int = 0,
+              descending: bool = False, stream=None) -> None:
+    """Sorts host buffers (pointers or pinned torch tensors) through d_buffer."""
+    st = lib().gbsort_sort_host(key_type_id(key_type), int(descending), _ptr(h_keys), _ptr(h_values),
+                                value_bytes if h_values is not None else 0, n, _ptr(d_buffer), buffer_bytes,
+                                _stream(stream))
+    _check(st, "host sort")
+
+
+def set_wait_limit_ns(ns: int) -> None:
+    lib().gbsort_set_wait_limit_ns(ns)
+
+
+def get_wait_limit_ns() -> int:
+    return lib().gbsort_get_wait_limit_ns()
+
+
+def probe_wait_timeout(scratch, limit_ns: int, stream=None) -> int:
+    return lib().gbsort_probe_wait_timeout(_ptr(scratch), limit_ns, _stream(stream))
+
+
+def sm_count() -> int:
+    return lib().gbsort_device_sm_count()

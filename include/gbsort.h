@@ -1,0 +1,217 @@
+/*
+ * gbsort.h — C ABI of the GB300 (sm_103a) onesweep LSD radix sort.
+ *
+ * Every entry point is a plain C function over raw device pointers and sizes,
+ * so any FFI (ctypes, cgo, JNI, N-API) and the header-only C++ shim in
+ * include/rsort/rsort.cuh can bind it.  No CUDA type appears in a signature:
+ * streams are passed as `void*` (a cudaStream_t, or NULL for the legacy
+ * default stream).
+ *
+ * Reference interface replaced (AwardOfSky/CUDA-Fast-Sort, "rsort" v0.4.0):
+ *   include/rsort/rsort.cuh:13-30   rsort::sort                  -> gbsort_sort_keys
+ *   include/rsort/rsort.cuh:33-50   rsort::sort_descending       -> gbsort_sort_keys(descending=1)
+ *   include/rsort/rsort.cuh:53-71   rsort::sort_pairs            -> gbsort_sort_pairs
+ *   include/rsort/rsort.cuh:74-92   rsort::sort_pairs_descending -> gbsort_sort_pairs(descending=1)
+ *   include/rsort/detail/radix_kernel.cuh:486-507  size query (workspace == NULL
+ *       writes the required bytes to *temp_bytes and returns, no device work)
+ *
+ * Protocol (same as rsort): call once with workspace == NULL to learn
+ * *temp_bytes, allocate that many device bytes, call again with the
+ * workspace; keys (and values) are sorted in place, ping-ponging through the
+ * workspace.  The library allocates no device memory on this path.
+ *
+ * Deliberate differences from rsort, all in the caller's favour:
+ *   - the stream argument is honoured (rsort replaces it by a private stream
+ *     and replays a graph on the legacy stream, radix_kernel.cuh:583-601);
+ *   - n == 0 is a no-op (rsort underflows, radix_kernel.cuh:385);
+ *   - errors come back as a gbsort_status instead of being dropped;
+ *   - device-side waits are bounded: a stalled lookback sets an error word
+ *     in the workspace (read with gbsort_workspace_status) instead of hanging.
+ */
+#ifndef GBSORT_H
+#define GBSORT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Key types.  The 13 types rsort validates (benchmark/validate_sort.cuh:36-40).
+ * GBSORT_KEY_F128 is `long double` on platforms where it is 16 bytes: the key
+ * is ordered as a raw 128-bit pattern with the float twiddle applied at bit
+ * 127, exactly as rsort does (detail/radix_kernel.cuh:351-356 reinterprets the
+ * buffer as unsigned __int128; detail/tuning.cuh:356-357 twiddles it). */
+typedef enum gbsort_key_type {
+    GBSORT_KEY_U8 = 0,
+    GBSORT_KEY_U16 = 1,
+    GBSORT_KEY_U32 = 2,
+    GBSORT_KEY_U64 = 3,
+    GBSORT_KEY_U128 = 4,
+    GBSORT_KEY_I8 = 5,
+    GBSORT_KEY_I16 = 6,
+    GBSORT_KEY_I32 = 7,
+    GBSORT_KEY_I64 = 8,
+    GBSORT_KEY_I128 = 9,
+    GBSORT_KEY_F32 = 10,
+    GBSORT_KEY_F64 = 11,
+    GBSORT_KEY_F128 = 12,
+    GBSORT_KEY_COUNT = 13
+} gbsort_key_type;
+
+typedef enum gbsort_status {
+    GBSORT_OK = 0,
+    GBSORT_ERR_INVALID_ARGUMENT = 1,   /* bad key type, value size, null pointer */
+    GBSORT_ERR_WORKSPACE_TOO_SMALL = 2,/* *temp_bytes smaller than required     */
+    GBSORT_ERR_CUDA = 3,               /* a CUDA runtime call or launch failed  */
+    GBSORT_ERR_TIMEOUT = 4,            /* a bounded device wait ran out         */
+    GBSORT_ERR_UNSUPPORTED = 5,        /* no device of compute capability 10.3  */
+    GBSORT_ERR_BUDGET = 6,             /* server: request exceeds memory budget */
+    GBSORT_ERR_NOT_READY = 7,          /* server: result not yet available      */
+    GBSORT_ERR_INTERNAL = 8            /* a device-side bounds check fired      */
+} gbsort_status;
+
+/* Bytes of one key of the given type (0 for an unknown type). */
+size_t gbsort_key_bytes(int key_type);
+
+/* Human-readable text for a status code (static storage). */
+const char* gbsort_status_string(int status);
+
+/* Library version string, e.g. "gbsort 1.0 sm_103a". */
+const char* gbsort_version(void);
+
+/* Text of the last CUDA failure seen by this thread ("" if none). */
+const char* gbsort_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* Plain sort: the drop-in for rsort::sort / sort_descending /              */
+/* sort_pairs / sort_pairs_descending (include/rsort/rsort.cuh:13-92).       */
+/* ------------------------------------------------------------------------ */
+
+/* Keys-only sort, in place.  workspace == NULL: writes the required bytes to
+ * *temp_bytes and returns GBSORT_OK without touching the device.  Otherwise
+ * *temp_bytes must hold the workspace size (>= the required bytes). */
+int gbsort_sort_keys(int key_type, int descending, void* d_keys,
+                     size_t* temp_bytes, void* d_workspace, size_t n,
+                     void* stream);
+
+/* Key-value sort, in place.  value_bytes is the size of one value: 1, 2, 4,
+ * 8 or 16 (values are moved as raw bytes, so any trivially copyable type of
+ * those sizes works).  Equal keys keep their input order (stable). */
+int gbsort_sort_pairs(int key_type, int descending, void* d_keys,
+                      void* d_values, size_t value_bytes, size_t* temp_bytes,
+                      void* d_workspace, size_t n, void* stream);
+
+/* Typed convenience entry points (same semantics as above). */
+#define GBSORT_DECLARE_TYPED(name)                                              \
+    int gbsort_sort_##name(void* d_keys, size_t* temp_bytes, void* d_workspace, \
+                           size_t n, void* stream);                             \
+    int gbsort_sort_##name##_desc(void* d_keys, size_t* temp_bytes,             \
+                                  void* d_workspace, size_t n, void* stream);   \
+    int gbsort_sort_pairs_##name(void* d_keys, void* d_values,                  \
+                                 size_t value_bytes, size_t* temp_bytes,        \
+                                 void* d_workspace, size_t n, void* stream);    \
+    int gbsort_sort_pairs_##name##_desc(void* d_keys, void* d_values,           \
+                                        size_t value_bytes, size_t* temp_bytes, \
+                                        void* d_workspace, size_t n,            \
+                                        void* stream);
+GBSORT_DECLARE_TYPED(u8)
+GBSORT_DECLARE_TYPED(u16)
+GBSORT_DECLARE_TYPED(u32)
+GBSORT_DECLARE_TYPED(u64)
+GBSORT_DECLARE_TYPED(u128)
+GBSORT_DECLARE_TYPED(i8)
+GBSORT_DECLARE_TYPED(i16)
+GBSORT_DECLARE_TYPED(i32)
+GBSORT_DECLARE_TYPED(i64)
+GBSORT_DECLARE_TYPED(i128)
+GBSORT_DECLARE_TYPED(f32)
+GBSORT_DECLARE_TYPED(f64)
+GBSORT_DECLARE_TYPED(f128)
+#undef GBSORT_DECLARE_TYPED
+
+/* Sort from HOST buffers: copies n keys (and values) from host memory into
+ * the caller's device buffer d_buffer, sorts them there and copies the result
+ * back, all on `stream`, then synchronizes the stream.  d_buffer must hold
+ * gbsort_host_buffer_bytes(...) bytes (keys + values + workspace); pinned host
+ * memory gives full copy bandwidth.  No allocation happens inside. */
+size_t gbsort_host_buffer_bytes(int key_type, size_t value_bytes, size_t n);
+int gbsort_sort_host(int key_type, int descending, void* h_keys,
+                     void* h_values, size_t value_bytes, size_t n,
+                     void* d_buffer, size_t buffer_bytes, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Workspace status and bounded waits                                       */
+/* ------------------------------------------------------------------------ */
+
+/* Synchronizes `stream`, then reads the error word the last sort on this
+ * workspace left (GBSORT_OK or GBSORT_ERR_TIMEOUT).  Needs the n, key type and
+ * value size of that sort to locate the word. */
+int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n,
+                            void* d_workspace, void* stream);
+
+/* Upper bound, in nanoseconds, on any single device-side wait (lookback spin
+ * or TMA barrier) of later launches.  Default 2e9 (2 s).  Process-wide. */
+void gbsort_set_wait_limit_ns(uint64_t ns);
+uint64_t gbsort_get_wait_limit_ns(void);
+
+/* Runs one bounded wait, on the device, on a status word that nothing ever
+ * publishes, with the given limit; returns GBSORT_ERR_TIMEOUT when the wait
+ * gave up (the expected outcome) and GBSORT_OK otherwise.  d_scratch must
+ * point to 64 bytes of device memory.  Exercises the failure path of the
+ * lookback without stalling any sort. */
+int gbsort_probe_wait_timeout(void* d_scratch, uint64_t limit_ns,
+                              void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Introspection used by the benchmark                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Geometry the plain sort picks for (key type, value size, n). */
+typedef struct gbsort_plan_info {
+    uint32_t passes;          /* digit passes (key bytes)                    */
+    uint32_t radix_bits;      /* bits per digit (8)                          */
+    uint32_t tile_items;      /* keys per tile                               */
+    uint32_t threads;         /* threads per CTA of the pass kernel          */
+    uint32_t items_per_thread;
+    uint32_t num_tiles;
+    uint32_t pass_ctas;       /* persistent CTAs of the pass kernel          */
+    uint32_t hist_ctas;       /* CTAs of the histogram kernel                */
+    uint32_t status_word_bytes; /* 4 or 8                                    */
+    uint32_t kernel_launches; /* launches (plus one memset node) per sort    */
+    uint64_t workspace_bytes;
+} gbsort_plan_info;
+
+int gbsort_plan(int key_type, size_t value_bytes, size_t n,
+                gbsort_plan_info* out);
+
+/* Same as gbsort_sort_pairs (d_values may be NULL with value_bytes 0), but
+ * records a CUDA event around every kernel on `stream` and, after
+ * synchronizing, writes the per-kernel device milliseconds to ms_out:
+ * ms_out[0] = histogram kernel, ms_out[1 + p] = digit pass p.  ms_cap is the
+ * capacity of ms_out; *n_ms receives the number of entries written. */
+int gbsort_sort_timed(int key_type, int descending, void* d_keys,
+                      void* d_values, size_t value_bytes, void* d_workspace,
+                      size_t temp_bytes, size_t n, void* stream,
+                      float* ms_out, int ms_cap, int* n_ms);
+
+/* Fills d_out with n synthetic keys on the device (seeded, deterministic):
+ *   dist 0: splitmix64 stream, full-range bits of the key width
+ *   dist 1: float32 N(0,1) with 1% -0.0, 0.1% +/-inf, 0.01% quiet NaN
+ *   dist 2: uint64, upper 32 bits from 256 distinct values, lower uniform
+ *   dist 3: ascending index values (key i = i)
+ *   dist 4: rsort init_keys "random" mode (mix32 of i ^ seed)
+ *   dist 5: rsort init_keys "byte_skip" mode
+ * key_bytes is the width written (1, 2, 4, 8 or 16). */
+int gbsort_generate(int dist, size_t key_bytes, void* d_out, size_t n,
+                    uint64_t seed, void* stream);
+
+/* Number of SMs of the current device, 0 without a device. */
+int gbsort_device_sm_count(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* GBSORT_H */
