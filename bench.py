@@ -320,6 +320,45 @@ def bench_gbsort(args, cfg, world, rank, local):
         sort_bytes / (mean_sort_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
         "frac": round(sort_bytes / (mean_sort_ms / 1e3) / 1e9 / hbm, 4)}
 
+    # comparator: CUB DeviceRadixSort (toolkit) on the same buffers, same timing
+    cub = None
+    cub_kind = {"c2b": 0, "c1": 0, "c2a": 1, "c3a": 2}.get(args.config)
+    cub_lib_path = os.path.join(PKG, "lib", "libcubcompare.so")
+    if rank == 0 and cub_kind is not None and os.path.exists(cub_lib_path) and not args.no_cub:
+        import ctypes
+
+        cl = ctypes.CDLL(cub_lib_path)
+        cl.cubcmp_sort.restype = ctypes.c_int
+        cl.cubcmp_sort.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + [
+            ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p,
+            ctypes.POINTER(ctypes.c_int)]
+        k_alt = torch.empty(n * kbytes, dtype=torch.uint8, device=dev)
+        v_alt = torch.empty(max(1, n * vb), dtype=torch.uint8, device=dev)
+        ctb = ctypes.c_size_t(0)
+        sel = ctypes.c_int(0)
+        vptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        cl.cubcmp_sort(cub_kind, int(desc), keys[0].data_ptr(), k_alt.data_ptr(), vptr(vals[0]), v_alt.data_ptr(), n,
+                       None, ctypes.byref(ctb), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(sel))
+        ctemp = torch.empty(max(1, ctb.value), dtype=torch.uint8, device=dev)
+        cub_ms = []
+        for i in range(args.warmup + min(args.steps, 30)):
+            prepare(i & 1, 555 + i)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            rc = cl.cubcmp_sort(cub_kind, int(desc), keys[i & 1].data_ptr(), k_alt.data_ptr(), vptr(vals[i & 1]),
+                                v_alt.data_ptr(), n, ctemp.data_ptr(), ctypes.byref(ctb),
+                                ctypes.c_void_p(stream.cuda_stream), ctypes.byref(sel))
+            b.record(stream)
+            if rc != 0:
+                raise RuntimeError(f"CUB comparator failed: {rc}")
+            if i >= args.warmup:
+                cub_ms.append((a, b))
+        torch.cuda.synchronize()
+        cms = statistics.mean(a.elapsed_time(b) for a, b in cub_ms)
+        cub = {"value": round(n / (cms / 1e3) / 1e9, 3), "unit": "Gkeys/s", "ms_per_step": round(cms, 4),
+               "impl": "cub::DeviceRadixSort (CUDA 13.0 toolkit, DoubleBuffer)", "steps": len(cub_ms)}
+        del k_alt, v_alt, ctemp
+
     # e2e: host buffers through the C ABI, copies inside the timed region
     e2e = None
     if rank == 0 or world > 1:
@@ -378,6 +417,7 @@ def bench_gbsort(args, cfg, world, rank, local):
         "sort_roofline": sort_roofline,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "comparators": {"cub": cub},
         "clocks": clk,
         "gpu_launches": args.steps * (passes + 2 + (1 if vb else 0)),
         "gpu_launches_note": "per step: generate (+values) + upsweep + one pass per key byte; plus one memset node",
@@ -396,6 +436,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cub", action="store_true", help="skip the CUB comparator")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # timing rule: at least 3 warm-up steps
     world, rank, local = dist_init()

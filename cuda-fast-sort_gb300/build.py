@@ -42,11 +42,12 @@ def _newest(paths) -> float:
     return max((os.path.getmtime(p) for p in paths), default=0.0)
 
 
-def _compile(src: str, headers_mtime: float, force: bool, verbose: bool) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src: str, headers_mtime: float, force: bool, verbose: bool, obj_dir: str,
+             defines: list[str]) -> str:
+    obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(headers_mtime, os.path.getmtime(src)):
         return obj
-    cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + NVCC_FLAGS + [f"-D{d}" for d in defines] + ["-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -57,24 +58,49 @@ def _compile(src: str, headers_mtime: float, force: bool, verbose: bool) -> str:
     return obj
 
 
-def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+def build(jobs: int | None = None, force: bool = False, verbose: bool = False, defines: list[str] | None = None,
+          out_dir: str | None = None) -> str:
+    """Builds the library; `defines` (-D...) and `out_dir` produce a variant
+    build (objects and libgbsort.so under out_dir) for tuning sweeps."""
+    defines = defines or []
+    obj_dir = os.path.join(out_dir, "obj") if out_dir else BUILD
+    lib = os.path.join(out_dir, "libgbsort.so") if out_dir else LIB
+    os.makedirs(obj_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     headers = (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
                + glob.glob(os.path.join(INCLUDE, "*.h")))
     hm = _newest(headers + [os.path.abspath(__file__)])
     jobs = jobs or max(1, min(len(sources), os.cpu_count() or 4))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(lambda s: _compile(s, hm, force, verbose), sources))
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
-        tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, hm, force, verbose, obj_dir, defines), sources))
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < _newest(objs):
+        tmp = lib + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
+
+
+CUB_SRC = os.path.join(PKG, "compare", "cub_compare.cu")
+CUB_LIB = os.path.join(LIBDIR, "libcubcompare.so")
+
+
+def build_cub_compare() -> str:
+    """Benchmark comparator: cub::DeviceRadixSort from the CUDA toolkit, built
+    as its own library (not part of libgbsort)."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    if os.path.exists(CUB_LIB) and os.path.getmtime(CUB_LIB) >= os.path.getmtime(CUB_SRC):
+        return CUB_LIB
+    tmp = CUB_LIB + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", CUB_SRC, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CUB comparator build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CUB_LIB)
+    return CUB_LIB
 
 
 SHIM_TEST_SRC = os.path.join(REPO, "tests", "cpp", "rsort_shim_test.cpp")
@@ -101,5 +127,7 @@ if __name__ == "__main__":
     ap.add_argument("--jobs", type=int, default=None)
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("-D", dest="defines", action="append", default=[], help="extra preprocessor define")
+    ap.add_argument("--out-dir", default=None, help="variant build directory")
     a = ap.parse_args()
-    print(build(a.jobs, a.force, a.verbose))
+    print(build(a.jobs, a.force, a.verbose, a.defines, a.out_dir))

@@ -15,11 +15,36 @@ enum KeyKind : int { KIND_UNSIGNED = 0, KIND_SIGNED = 1, KIND_FLOAT = 2 };
 // Error bits of the workspace error word.
 enum : uint32_t { ERRBIT_TIMEOUT = 1u, ERRBIT_BOUNDS = 2u };
 
-// Device-side bounds checks on staging ranks and scatter positions: a failed
-// check records ERRBIT_BOUNDS and skips the access instead of faulting.
+// Device-side bounds check on every scatter position (one compare per key): a
+// failed check records ERRBIT_BOUNDS and skips the store instead of faulting.
 #ifndef GBSORT_BOUNDS_CHECK
 #define GBSORT_BOUNDS_CHECK 1
 #endif
+// Debug-only extra check of the shared-memory staging rank (always < tile by
+// construction).
+#ifndef GBSORT_DEBUG_CHECKS
+#define GBSORT_DEBUG_CHECKS 0
+#endif
+// Rank atomics: 1 = only the leader lane of a digit group issues it (a
+// divergent branch), 0 = every lane issues it and non-leaders add 0.
+#ifndef GBSORT_RANK_LEADER_BRANCH
+#define GBSORT_RANK_LEADER_BRANCH 1
+#endif
+
+template <bool B> struct BoolTag { static constexpr bool value = B; };
+template <int I> struct IntTag { static constexpr int value = I; };
+
+// Compile-time loop: f(IntTag<U>{}) for U in [U0, N).
+template <int U0, int N>
+struct StaticFor {
+    template <class F>
+    __device__ __forceinline__ static void run(F&& f) {
+        if constexpr (U0 < N) {
+            f(IntTag<U0>{});
+            StaticFor<U0 + 1, N>::run(f);
+        }
+    }
+};
 
 // After a wait ran out, copies still in flight are drained for at most this
 // long before a CTA leaves (a bulk copy from valid memory lands in microseconds).
@@ -117,6 +142,18 @@ __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
+// Same loads without a compiler memory barrier, so a window of them issues
+// back to back (used for the lookback window).
+__device__ __forceinline__ uint32_t ld_relaxed_nb(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint64_t ld_relaxed_nb(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
 __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -128,6 +165,56 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
+}
+
+// Mask of the lanes of this warp holding the same 8-bit digit.  Three ways to
+// build it, identical results, each loading a different SM pipe:
+//   RANK_BALLOT: 8 ballots, one per digit bit (integer ALU pipe)
+//   RANK_MATCH:  the MATCH instruction (its own, low-throughput pipe)
+//   RANK_OR:     lanes OR their bit into a per-warp shared word of the digit
+//                and read it back (load/store pipe)
+// GBSORT_RANK_PATTERN lists the method per column of items (4 bits each,
+// column u uses nibble u % GBSORT_RANK_PATTERN_LEN), spreading the work.
+enum RankMethod : int { RANK_BALLOT = 0, RANK_MATCH = 1, RANK_OR = 2 };
+#ifndef GBSORT_RANK_PATTERN
+#define GBSORT_RANK_PATTERN 0x2  // every column: shared-memory OR (fastest on GB300)
+#define GBSORT_RANK_PATTERN_LEN 1
+#endif
+__host__ __device__ constexpr int rank_method(int column) {
+    return int((uint64_t(GBSORT_RANK_PATTERN) >> (4 * (column % GBSORT_RANK_PATTERN_LEN))) & 0xF);
+}
+__host__ __device__ constexpr bool rank_uses_or(int ipt) {
+    for (int u = 0; u < ipt; ++u)
+        if (rank_method(u) == RANK_OR) return true;
+    return false;
+}
+
+__device__ __forceinline__ uint32_t match_ballot(uint32_t d) {
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+        const uint32_t m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+        peers &= ((d >> bit) & 1u) ? m : ~m;
+    }
+    return peers;
+}
+
+// `mb`: this warp's 256 zeroed shared words; left zeroed on return.
+__device__ __forceinline__ uint32_t match_or(uint32_t d, uint32_t* mb, int lane, uint32_t lt) {
+    atomicOr(&mb[d], 1u << lane);
+    __syncwarp();
+    const uint32_t peers = mb[d];
+    __syncwarp();
+    if ((peers & lt) == 0) mb[d] = 0u;  // the group's lowest lane clears
+    __syncwarp();
+    return peers;
+}
+
+template <int METHOD>
+__device__ __forceinline__ uint32_t warp_match_digit(uint32_t d, uint32_t* mb, int lane, uint32_t lt) {
+    if constexpr (METHOD == RANK_MATCH) return __match_any_sync(0xffffffffu, d);
+    else if constexpr (METHOD == RANK_OR) return match_or(d, mb, lane, lt);
+    else return match_ballot(d);
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -223,6 +310,34 @@ __device__ __forceinline__ W wait_status(const W* addr, uint32_t epoch, uint64_t
             return Codec::GLOBAL;
         }
     }
+}
+
+// Decoupled lookback for one digit bin of tile `cur` over a [tile][256] status
+// array: reads WIN predecessors' words at once (one L2 round trip per window
+// instead of per tile), then sums them nearest-first up to the first
+// inclusive (GLOBAL) word, re-polling (bounded) any word not yet published.
+// Tile 0 always publishes GLOBAL, so the walk ends there at the latest.
+template <class Codec, int WIN, class W>
+__device__ __forceinline__ unsigned long long lookback_window(const W* status, uint32_t cur, int bin,
+                                                             uint32_t epoch, uint64_t limit_ns, uint32_t* err) {
+    unsigned long long prefix = 0;
+    int64_t j = int64_t(cur) - 1;
+    while (j >= 0) {
+        W w[WIN];
+#pragma unroll
+        for (int i = 0; i < WIN; ++i)
+            w[i] = (j - i >= 0) ? ld_relaxed_nb(status + size_t(j - i) * 256 + bin) : W(0);
+#pragma unroll
+        for (int i = 0; i < WIN; ++i) {
+            if (j - i < 0) return prefix;
+            W x = w[i];
+            if (!Codec::ready(x, epoch)) x = wait_status<Codec>(status + size_t(j - i) * 256 + bin, epoch, limit_ns, err);
+            prefix += Codec::value(x);
+            if (Codec::is_global(x)) return prefix;
+        }
+        j -= WIN;
+    }
+    return prefix;
 }
 
 // Exclusive scan of one value per thread over threads [0, 256) of the block.

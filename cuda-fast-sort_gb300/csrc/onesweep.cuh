@@ -150,7 +150,9 @@ struct PassGeom {
     static constexpr size_t SCAN32_OFF = SCAN64_OFF + 64;         // u32 [8]
     static constexpr size_t MBAR_OFF = SCAN32_OFF + 64;           // u64 [2]
     static constexpr size_t TILEID_OFF = MBAR_OFF + 16;           // u32 [2]
-    static constexpr size_t SMEM_BYTES = TILEID_OFF + 16;
+    static constexpr size_t BINB32_OFF = TILEID_OFF + 16;         // u32 [256]
+    static constexpr size_t MATCH_OFF = BINB32_OFF + 256 * 4;     // u32 [WARPS][256] when RANK_OR is used
+    static constexpr size_t SMEM_BYTES = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);
     static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
     static_assert(TILE % 16 == 0, "tile starts must stay 16-byte aligned");
 };
@@ -171,6 +173,11 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     uint32_t* scan32 = reinterpret_cast<uint32_t*>(smem + G::SCAN32_OFF);
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + G::MBAR_OFF);
     volatile uint32_t* tile_slot = reinterpret_cast<volatile uint32_t*>(smem + G::TILEID_OFF);
+    uint32_t* binb32 = reinterpret_cast<uint32_t*>(smem + G::BINB32_OFF);
+    uint32_t* match_scratch = reinterpret_cast<uint32_t*>(smem + G::MATCH_OFF);
+    if constexpr (rank_uses_or(IPT)) {
+        for (int i = threadIdx.x; i < G::WARPS * 256; i += THREADS) match_scratch[i] = 0u;
+    }
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t T = p.num_tiles;
@@ -314,75 +321,104 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         }
         __syncthreads();
 
-        // ---- rank: warp match + popc + one shared atomic per digit group
+        // ---- rank: warp match + popc + one shared atomic per digit group;
+        // the group's base comes from the leader (lowest lane) by shuffle.
         uint32_t rank[IPT];
         const uint32_t lt = lanemask_lt();
-#pragma unroll
-        for (int u = 0; u < IPT; ++u) {
+        uint32_t* mb = match_scratch + warp * 256;
+        StaticFor<0, IPT>::run([&](auto uc) {
+            constexpr int u = decltype(uc)::value;
             const uint32_t d = digit_of(keys[u], pass);
-            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
             const uint32_t below = __popc(peers & lt);
-            uint32_t off = 0;
-            if (below == 0) off = atomicAdd(&wh[d], uint32_t(__popc(peers)));
-            off = __shfl_sync(0xffffffffu, off, __ffs(peers) - 1);
-            rank[u] = off + below;
-        }
+#if GBSORT_RANK_LEADER_BRANCH
+            uint32_t old = 0;
+            if (below == 0) old = atomicAdd(&wh[d], uint32_t(__popc(peers)));
+#else
+            // every lane issues the atomic, non-leaders add 0: no divergence
+            const uint32_t old = atomicAdd(&wh[d], below == 0 ? uint32_t(__popc(peers)) : 0u);
+#endif
+            rank[u] = __shfl_sync(0xffffffffu, old, __ffs(peers) - 1) + below;
+        });
 
-        // ---- decoupled lookback (bin owners), GLOBAL publication, bases
-        if (tid < 256) {
-            unsigned long long prefix = 0;
-            if (cur > 0) {
-                uint32_t j = cur - 1;
-                const W* sp = status + size_t(j) * 256 + tid;
-                for (;;) {
-                    const W w = wait_status<Codec>(sp, epoch, p.wait_limit_ns, p.err);
-                    prefix += Codec::value(w);
-                    if (Codec::is_global(w) || j == 0) break;
-                    --j;
-                    sp -= 256;
-                }
-                if (cur + 1 < T)
-                    st_relaxed(status + size_t(cur) * 256 + tid,
-                               Codec::pack(Codec::GLOBAL, epoch, prefix + valid_total));
-            }
-            binb[tid] = gexcl[tid] + prefix - excl;
-        }
-        __syncthreads();
-
-        // ---- stage at rank (this buffer's input is already in registers)
+        // ---- stage at rank: every thread read its input before the first
+        // barrier of this tile, so the buffer is free; keys/ranks die here,
+        // which leaves the registers to the lookback window.
+        bool bad = false;
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
-#if GBSORT_BOUNDS_CHECK
+#if GBSORT_DEBUG_CHECKS
             if (rank[u] >= uint32_t(G::TILE)) {
-                atomicOr(p.err, ERRBIT_BOUNDS);
+                bad = true;
                 continue;
             }
 #endif
             sk[rank[u]] = keys[u];
             if constexpr (PAIRS) sv[rank[u]] = vals[u];
         }
+
+        // ---- decoupled lookback (bin owners), GLOBAL publication, bases
+        if (tid < 256) {
+            unsigned long long prefix = 0;
+            if (cur > 0) {
+                prefix = lookback_window<Codec, PassShape<KB, VB>::LOOKBACK_WINDOW>(status, cur, tid, epoch,
+                                                                                  p.wait_limit_ns, p.err);
+                if (cur + 1 < T)
+                    st_relaxed(status + size_t(cur) * 256 + tid,
+                               Codec::pack(Codec::GLOBAL, epoch, prefix + valid_total));
+            }
+            const unsigned long long base = gexcl[tid] + prefix - excl;
+            binb[tid] = base;
+            binb32[tid] = uint32_t(base);
+        }
         __syncthreads();
 
         // ---- coalesced write-out: thread-linear over the digit-sorted tile
         U* okeys = static_cast<U*>(p.keys_out);
         V* ovals = static_cast<V*>(p.vals_out);
-        const int tw_store = p.twiddle_store;
+        // Full tiles with 32-bit positions (n < 2^32) take a lean loop: one
+        // shared load of the key, of its 32-bit base, one wide-address store.
+        auto scatter32 = [&](auto twiddle_tag) {
+            constexpr bool TW = decltype(twiddle_tag)::value;
+            const uint32_t n32 = uint32_t(n);
 #pragma unroll
-        for (int u = 0; u < IPT; ++u) {
-            const uint32_t i = uint32_t(u * THREADS + tid);
-            if (full || i < cnt) {
+            for (int u = 0; u < IPT; ++u) {
+                const uint32_t i = uint32_t(u * THREADS + tid);
                 const U k = sk[i];
-                const unsigned long long pos = binb[digit_of(k, pass)] + i;
+                const uint32_t pos = binb32[digit_of(k, pass)] + i;
+                bool ok = true;
 #if GBSORT_BOUNDS_CHECK
-                if (pos >= n) {
-                    atomicOr(p.err, ERRBIT_BOUNDS);
-                    continue;
-                }
+                ok = pos < n32;
+                bad |= !ok;
 #endif
-                okeys[pos] = tw_store ? twiddle_out<U>(k, kind, desc) : k;
-                if constexpr (PAIRS) ovals[pos] = sv[i];
+                if (ok) {
+                    okeys[pos] = TW ? twiddle_out<U>(k, kind, desc) : k;
+                    if constexpr (PAIRS) ovals[pos] = sv[i];
+                }
+            }
+        };
+        if (full && n < 0xFFFFFFFFull) {
+            if (p.twiddle_store) scatter32(BoolTag<true>{});
+            else scatter32(BoolTag<false>{});
+        } else {
+            const int tw_store = p.twiddle_store;
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) {
+                const uint32_t i = uint32_t(u * THREADS + tid);
+                const U k = sk[i];  // i < TILE: always inside the staging buffer
+                const unsigned long long pos = binb[digit_of(k, pass)] + i;
+                bool ok = full || i < cnt;
+#if GBSORT_BOUNDS_CHECK
+                bad |= ok && pos >= n;
+                ok = ok && pos < n;
+#endif
+                if (ok) {
+                    okeys[pos] = tw_store ? twiddle_out<U>(k, kind, desc) : k;
+                    if constexpr (PAIRS) ovals[pos] = sv[i];
+                }
             }
         }
+        if (bad) atomicOr(p.err, ERRBIT_BOUNDS);
         __syncthreads();
         cur = next_tile;
         ++it;

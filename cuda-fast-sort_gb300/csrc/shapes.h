@@ -13,14 +13,28 @@ constexpr int HIST_THREADS = 1024;
 
 template <int KB, int VB>
 struct PassShape {
-    static constexpr int THREADS = 512;
+    static constexpr int THREADS = (KB <= 4 && VB == 0) ? 384 : 512;
     static constexpr int IPT =
-        KB <= 4 ? (VB == 0 ? 16 : VB <= 4 ? 10 : VB == 8 ? 8 : 6)
+        KB <= 4 ? (VB == 0 ? 24 : VB <= 4 ? 10 : VB == 8 ? 8 : 6)
       : KB == 8 ? (VB == 0 ? 10 : VB <= 4 ? 8 : VB == 8 ? 6 : 4)
       :           (VB == 0 ? 6 : 4);
     // Resident CTAs per SM the register allocation must allow.
     static constexpr int MIN_CTAS = 2;
+    // Predecessor tiles read per lookback round trip.
+    static constexpr int LOOKBACK_WINDOW = 8;
 };
+
+// Build-time override of the 4-byte keys-only shape, for tuning sweeps
+// (-DGBSORT_SHAPE_K4V0_THREADS=.. -DGBSORT_SHAPE_K4V0_IPT=.. -DGBSORT_SHAPE_K4V0_MIN_CTAS=..).
+#if defined(GBSORT_SHAPE_K4V0_THREADS)
+template <>
+struct PassShape<4, 0> {
+    static constexpr int THREADS = GBSORT_SHAPE_K4V0_THREADS;
+    static constexpr int IPT = GBSORT_SHAPE_K4V0_IPT;
+    static constexpr int MIN_CTAS = GBSORT_SHAPE_K4V0_MIN_CTAS;
+    static constexpr int LOOKBACK_WINDOW = GBSORT_SHAPE_K4V0_WINDOW;
+};
+#endif
 
 // Value-size index used by the dispatch tables: 0,1,2,4,8,16 bytes -> 0..5.
 inline int value_index(int vb) {

@@ -17,7 +17,8 @@ import os
 from dataclasses import dataclass
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG_DIR, "lib", "libgbsort.so")
+# GBSORT_LIB selects another build of the same library (e.g. a tuning variant).
+LIB_PATH = os.environ.get("GBSORT_LIB") or os.path.join(PKG_DIR, "lib", "libgbsort.so")
 
 KEY_TYPES = {
     "u8": 0, "u16": 1, "u32": 2, "u64": 3, "u128": 4,
