@@ -67,5 +67,6 @@ int prepare_kernel(const KernelEntry& e); // cudaFuncSetAttribute once per devic
 
 uint64_t wait_limit_ns();
 void set_last_error(const char* what, cudaError_t err);
+void set_last_error_text(const char* text);
 
 }  // namespace gbsort

@@ -150,6 +150,8 @@ void set_last_error(const char* what, cudaError_t err) {
     g_last_error = std::string(what) + ": " + cudaGetErrorString(err);
 }
 
+void set_last_error_text(const char* text) { g_last_error = text; }
+
 int device_sm_count() {
     DeviceFacts* f = facts();
     return f ? f->sms : 0;

@@ -131,6 +131,21 @@ GBSORT_DECLARE_TYPED(f64)
 GBSORT_DECLARE_TYPED(f128)
 #undef GBSORT_DECLARE_TYPED
 
+/* Keys-only sort that allocates nothing and takes no workspace.  No
+ * counterpart in the reference (rsort always needs a caller workspace).  For
+ * callers that may not allocate device memory where they sort — cudaMalloc /
+ * cudaFree can block or synchronize the device, and some hosts own every
+ * device byte or give a library a fixed budget.  The scratch is a 16 MiB
+ * static device array inside the library, held by every GPU that loads it
+ * until exit.  Limit: the sort fits when the size query reports <= 16 MiB
+ * (about 4.0 M 4-byte, 2.0 M 8-byte or 1.0 M 16-byte keys); larger n returns
+ * GBSORT_ERR_WORKSPACE_TOO_SMALL with no device work.  The first call on a
+ * device looks up the array's address on that device: make it before any
+ * stream capture there.  All calls share the array (the sort re-clears what
+ * must start at zero); calls that overlap on the GPU race, so order them. */
+int gbsort_sort_keys_noalloc(int key_type, int descending, void* d_keys,
+                             size_t n, void* stream);
+
 /* Sort from HOST buffers: copies n keys (and values) from host memory into
  * the caller's device buffer d_buffer, sorts them there and copies the result
  * back, all on `stream`, then synchronizes the stream.  d_buffer must hold
