@@ -28,7 +28,7 @@ INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
-                     "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
+                     "-I", INCLUDE, "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:
@@ -43,11 +43,11 @@ def _newest(paths) -> float:
 
 
 def _compile(src: str, headers_mtime: float, force: bool, verbose: bool, obj_dir: str,
-             defines: list[str]) -> str:
+             defines: list[str], src_dir: str = CSRC) -> str:
     obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(headers_mtime, os.path.getmtime(src)):
         return obj
-    cmd = [nvcc()] + NVCC_FLAGS + [f"-D{d}" for d in defines] + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + NVCC_FLAGS + ["-I", src_dir] + [f"-D{d}" for d in defines] + ["-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -59,21 +59,22 @@ def _compile(src: str, headers_mtime: float, force: bool, verbose: bool, obj_dir
 
 
 def build(jobs: int | None = None, force: bool = False, verbose: bool = False, defines: list[str] | None = None,
-          out_dir: str | None = None) -> str:
-    """Builds the library; `defines` (-D...) and `out_dir` produce a variant
-    build (objects and libgbsort.so under out_dir) for tuning sweeps."""
+          out_dir: str | None = None, csrc: str | None = None) -> str:
+    """Builds the library; `defines` (-D...), `out_dir` and `csrc` (another
+    source directory) produce a variant build for tuning experiments."""
     defines = defines or []
+    src_dir = csrc or CSRC
     obj_dir = os.path.join(out_dir, "obj") if out_dir else BUILD
     lib = os.path.join(out_dir, "libgbsort.so") if out_dir else LIB
     os.makedirs(obj_dir, exist_ok=True)
     os.makedirs(os.path.dirname(lib), exist_ok=True)
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
-    headers = (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+    sources = sorted(glob.glob(os.path.join(src_dir, "*.cu")) + glob.glob(os.path.join(src_dir, "*.cpp")))
+    headers = (glob.glob(os.path.join(src_dir, "*.cuh")) + glob.glob(os.path.join(src_dir, "*.h"))
                + glob.glob(os.path.join(INCLUDE, "*.h")))
     hm = _newest(headers + [os.path.abspath(__file__)])
     jobs = jobs or max(1, min(len(sources), os.cpu_count() or 4))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(lambda s: _compile(s, hm, force, verbose, obj_dir, defines), sources))
+        objs = list(ex.map(lambda s: _compile(s, hm, force, verbose, obj_dir, defines, src_dir), sources))
     if force or not os.path.exists(lib) or os.path.getmtime(lib) < _newest(objs):
         tmp = lib + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"]
@@ -129,5 +130,6 @@ if __name__ == "__main__":
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("-D", dest="defines", action="append", default=[], help="extra preprocessor define")
     ap.add_argument("--out-dir", default=None, help="variant build directory")
+    ap.add_argument("--csrc", default=None, help="alternative source directory")
     a = ap.parse_args()
-    print(build(a.jobs, a.force, a.verbose, a.defines, a.out_dir))
+    print(build(a.jobs, a.force, a.verbose, a.defines, a.out_dir, a.csrc))

@@ -213,11 +213,15 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         if (PAIRS && vb) bulk_copy_g2s(buf + G::VAL_OFF, gvals_in + base, vb, &mbar[slot], pol);
     };
 
+    // Tile ids come from the pass's atomic counter two tiles ahead (thread 0
+    // holds the id after next), so the atomic's latency hides behind a tile.
+    uint32_t id_after_next = 0;
     __syncthreads();
     if (tid == 0) {
         const uint32_t t = atomicAdd(p.tile_counter, 1u);
         tile_slot[0] = t;
         if (t < T) issue_tile(t, 0);
+        id_after_next = t < T ? atomicAdd(p.tile_counter, 1u) : T;
     }
     __syncthreads();
     uint32_t cur = tile_slot[0];
@@ -228,12 +232,13 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     while (cur < T) {
         const int b = int(it & 1u);
         if (tid == 0) {
-            const uint32_t nt = atomicAdd(p.tile_counter, 1u);
+            const uint32_t nt = id_after_next;
             tile_slot[(it + 1) & 1u] = nt;
             next_issued = nt < T;
             if (next_issued) {
                 fence_proxy_async_smem();
                 issue_tile(nt, b ^ 1);
+                id_after_next = atomicAdd(p.tile_counter, 1u);
             }
         }
         const bool landed = mbar_wait_bounded(&mbar[b], (parity >> b) & 1u, p.wait_limit_ns, p.err);
@@ -303,6 +308,8 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
 
         // ---- per-bin tile totals, warp bases, early PARTIAL publication
         uint32_t total = 0, valid_total = 0;
+        constexpr int LBW = PassShape<KB, VB>::LOOKBACK_WINDOW;
+        W lb_pre[LBW];
         if (tid < 256) {
 #pragma unroll
             for (int w = 0; w < G::WARPS; ++w) {
@@ -313,6 +320,10 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
             valid_total = total - ((tid == 255) ? (uint32_t(G::TILE) - cnt) : 0u);
             st_relaxed(status + size_t(cur) * 256 + tid,
                        Codec::pack(cur == 0 ? Codec::GLOBAL : Codec::PARTIAL, epoch, valid_total));
+#if GBSORT_LOOKBACK_PREFETCH
+            // first lookback round trip overlaps the scan and the rank
+            lookback_prefetch<LBW>(status, cur, tid, lb_pre);
+#endif
         }
         const uint32_t excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
         if (tid < 256) {
@@ -361,8 +372,11 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         if (tid < 256) {
             unsigned long long prefix = 0;
             if (cur > 0) {
-                prefix = lookback_window<Codec, PassShape<KB, VB>::LOOKBACK_WINDOW>(status, cur, tid, epoch,
-                                                                                  p.wait_limit_ns, p.err);
+#if GBSORT_LOOKBACK_PREFETCH
+                prefix = lookback_finish<Codec, LBW>(status, cur, tid, lb_pre, epoch, p.wait_limit_ns, p.err);
+#else
+                prefix = lookback_window<Codec, LBW>(status, cur, tid, epoch, p.wait_limit_ns, p.err);
+#endif
                 if (cur + 1 < T)
                     st_relaxed(status + size_t(cur) * 256 + tid,
                                Codec::pack(Codec::GLOBAL, epoch, prefix + valid_total));

@@ -11,21 +11,58 @@ namespace gbsort {
 // Threads of the upsweep (global histogram) kernel.
 constexpr int HIST_THREADS = 1024;
 
+// Measured on a GB300 (pass kernel, bench.py configurations):
+//   4-byte keys only, 2^28:      384 x 24, 2 CTAs/SM  (67 Gkeys/s)
+//   f32 keys + u32 values, 2^28: 256 x 20, 2 CTAs/SM  (45 Gkeys/s)
+//   u64 keys + u64 values, 2^27: 256 x 10, 2 CTAs/SM  (12.9 Gkeys/s)
+//   u128 keys only, 2^26:        512 x 8,  1 CTA/SM   (5.9 Gkeys/s)
+// Other sizes follow by bytes per item within the same shared-memory budget
+// (two double-buffered tiles + per-warp counters and match words per CTA).
+struct ShapeRow {
+    int threads, ipt, min_ctas;
+};
+constexpr ShapeRow pass_shape_row(int kb, int vb) {
+    if (kb <= 4) {
+        if (vb == 0) return {384, 24, 2};
+        if (vb <= 4) return {256, 20, 2};
+        if (vb == 8) return {256, 12, 2};
+        return {256, 8, 2};
+    }
+    if (kb == 8) {
+        if (vb == 0) return {256, 20, 2};
+        if (vb <= 4) return {256, 12, 2};
+        if (vb == 8) return {256, 10, 2};
+        return {256, 6, 2};
+    }
+    if (vb == 0) return {512, 8, 1};
+    if (vb <= 8) return {256, 6, 2};
+    return {256, 4, 2};
+}
+
 template <int KB, int VB>
 struct PassShape {
-    static constexpr int THREADS = (KB <= 4 && VB == 0) ? 384 : 512;
-    static constexpr int IPT =
-        KB <= 4 ? (VB == 0 ? 24 : VB <= 4 ? 10 : VB == 8 ? 8 : 6)
-      : KB == 8 ? (VB == 0 ? 10 : VB <= 4 ? 8 : VB == 8 ? 6 : 4)
-      :           (VB == 0 ? 6 : 4);
+    static constexpr int THREADS = pass_shape_row(KB, VB).threads;
+    static constexpr int IPT = pass_shape_row(KB, VB).ipt;
     // Resident CTAs per SM the register allocation must allow.
-    static constexpr int MIN_CTAS = 2;
+    static constexpr int MIN_CTAS = pass_shape_row(KB, VB).min_ctas;
     // Predecessor tiles read per lookback round trip.
-    static constexpr int LOOKBACK_WINDOW = 8;
+    static constexpr int LOOKBACK_WINDOW = 4;
 };
 
-// Build-time override of the 4-byte keys-only shape, for tuning sweeps
-// (-DGBSORT_SHAPE_K4V0_THREADS=.. -DGBSORT_SHAPE_K4V0_IPT=.. -DGBSORT_SHAPE_K4V0_MIN_CTAS=..).
+// Build-time override of one (key bytes, value bytes) shape, for tuning
+// sweeps: -DGBSORT_SHAPE_KB=.. -DGBSORT_SHAPE_VB=.. -DGBSORT_SHAPE_THREADS=..
+// -DGBSORT_SHAPE_IPT=.. -DGBSORT_SHAPE_MIN_CTAS=..
+#if defined(GBSORT_SHAPE_KB)
+template <>
+struct PassShape<GBSORT_SHAPE_KB, GBSORT_SHAPE_VB> {
+    static constexpr int THREADS = GBSORT_SHAPE_THREADS;
+    static constexpr int IPT = GBSORT_SHAPE_IPT;
+    static constexpr int MIN_CTAS = GBSORT_SHAPE_MIN_CTAS;
+    static constexpr int LOOKBACK_WINDOW = 4;
+};
+#endif
+
+// Older form of the override for the 4-byte keys-only shape.
 #if defined(GBSORT_SHAPE_K4V0_THREADS)
 template <>
 struct PassShape<4, 0> {
