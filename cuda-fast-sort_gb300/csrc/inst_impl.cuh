@@ -1,30 +1,31 @@
 // inst_impl.cuh — explicit kernel instantiations for one key width.  Each
-// inst_k*.cu includes this with GBSORT_KB set, so the five widths compile as
-// five parallel translation units.
+// inst_k*.cu includes this with one width, so the five widths compile as
+// parallel translation units.
 #pragma once
 
 #include "onesweep.cuh"
+#include "segmented.cuh"
 #include "shapes.h"
 
 namespace gbsort {
 
-template <int KB, int VB, class W>
+template <int KB, int VB, class W, bool SEG>
 KernelEntry make_pass_entry() {
     using S = PassShape<KB, VB>;
     using G = PassGeom<KB, VB, S::THREADS, S::IPT>;
-    return KernelEntry{reinterpret_cast<const void*>(&onesweep_pass_kernel<KB, VB, W, S::THREADS, S::IPT>),
+    return KernelEntry{reinterpret_cast<const void*>(&onesweep_pass_kernel<KB, VB, W, S::THREADS, S::IPT, SEG>),
                        S::THREADS, S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
 }
 
 template <int KB>
 const KernelEntry* pass_entries_for() {
     static const KernelEntry e[6][2] = {
-        {make_pass_entry<KB, 0, uint32_t>(), make_pass_entry<KB, 0, uint64_t>()},
-        {make_pass_entry<KB, 1, uint32_t>(), make_pass_entry<KB, 1, uint64_t>()},
-        {make_pass_entry<KB, 2, uint32_t>(), make_pass_entry<KB, 2, uint64_t>()},
-        {make_pass_entry<KB, 4, uint32_t>(), make_pass_entry<KB, 4, uint64_t>()},
-        {make_pass_entry<KB, 8, uint32_t>(), make_pass_entry<KB, 8, uint64_t>()},
-        {make_pass_entry<KB, 16, uint32_t>(), make_pass_entry<KB, 16, uint64_t>()},
+        {make_pass_entry<KB, 0, uint32_t, false>(), make_pass_entry<KB, 0, uint64_t, false>()},
+        {make_pass_entry<KB, 1, uint32_t, false>(), make_pass_entry<KB, 1, uint64_t, false>()},
+        {make_pass_entry<KB, 2, uint32_t, false>(), make_pass_entry<KB, 2, uint64_t, false>()},
+        {make_pass_entry<KB, 4, uint32_t, false>(), make_pass_entry<KB, 4, uint64_t, false>()},
+        {make_pass_entry<KB, 8, uint32_t, false>(), make_pass_entry<KB, 8, uint64_t, false>()},
+        {make_pass_entry<KB, 16, uint32_t, false>(), make_pass_entry<KB, 16, uint64_t, false>()},
     };
     return &e[0][0];
 }
@@ -33,6 +34,52 @@ template <int KB>
 const KernelEntry* upsweep_entry_for() {
     static const KernelEntry e = {reinterpret_cast<const void*>(&upsweep_kernel<KB>), HIST_THREADS, 0, 0,
                                   static_cast<unsigned long>(HistGeom<KB>::SMEM_BYTES)};
+    return &e;
+}
+
+// ---- batched mode ---------------------------------------------------------
+// Small-segment CTA sorts: "S" = 256 threads x 8 items, "L" = 512 threads x
+// as many items as keep the two shared buffers within 128 KB.
+template <int KB, int VB>
+struct CtaShapes {
+    static constexpr int S_THREADS = 256, S_IPT = 8;
+    static constexpr int L_THREADS = 512;
+    static constexpr int L_ITEMS_RAW = 65536 / (KB + VB);
+    static constexpr int L_IPT = L_ITEMS_RAW / L_THREADS > 32 ? 32 : (L_ITEMS_RAW / L_THREADS < 4 ? 4 : L_ITEMS_RAW / L_THREADS);
+};
+
+template <int KB, int VB>
+void make_seg_entries(KernelEntry* out /* [3]: pass, cta S, cta L */) {
+    using C = CtaShapes<KB, VB>;
+    using GS = CtaSortGeom<KB, VB, C::S_THREADS, C::S_IPT>;
+    using GL = CtaSortGeom<KB, VB, C::L_THREADS, C::L_IPT>;
+    out[0] = make_pass_entry<KB, VB, uint32_t, true>();
+    out[1] = KernelEntry{reinterpret_cast<const void*>(&cta_sort_kernel<KB, VB, C::S_THREADS, C::S_IPT>),
+                         C::S_THREADS, C::S_IPT, GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)};
+    out[2] = KernelEntry{reinterpret_cast<const void*>(&cta_sort_kernel<KB, VB, C::L_THREADS, C::L_IPT>),
+                         C::L_THREADS, C::L_IPT, GL::TILE, static_cast<unsigned long>(GL::SMEM_BYTES)};
+}
+
+template <int KB>
+const KernelEntry* seg_entries_for() {
+    static KernelEntry e[6][3];
+    static const bool init = [] {
+        make_seg_entries<KB, 0>(e[0]);
+        make_seg_entries<KB, 1>(e[1]);
+        make_seg_entries<KB, 2>(e[2]);
+        make_seg_entries<KB, 4>(e[3]);
+        make_seg_entries<KB, 8>(e[4]);
+        make_seg_entries<KB, 16>(e[5]);
+        return true;
+    }();
+    (void)init;
+    return &e[0][0];
+}
+
+template <int KB>
+const KernelEntry* seg_upsweep_entry_for() {
+    static const KernelEntry e = {reinterpret_cast<const void*>(&seg_upsweep_kernel<KB>), SEG_UP_THREADS, 0, 0,
+                                  static_cast<unsigned long>(SegHistGeom<KB>::SMEM_BYTES)};
     return &e;
 }
 

@@ -132,32 +132,51 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
     }
 }
 
+
 // ---------------------------------------------------------------------------
 // Onesweep pass geometry and shared-memory layout.
 // ---------------------------------------------------------------------------
+// What thread 0 tells the CTA about a tile (one copy per buffer).
+struct TileInfo {
+    unsigned long long base;  // index of the tile's first element
+    uint32_t id;              // global tile id (>= num_tiles: no tile)
+    uint32_t cnt;             // elements in the tile
+    uint32_t seg;             // segment (batched mode)
+    uint32_t first;           // first tile of its segment / of the array
+    uint32_t last;            // last tile of its segment / of the array
+    uint32_t pad;
+};
+
 template <int KB, int VB, int THREADS, int IPT>
 struct PassGeom {
     static constexpr int WARPS = THREADS / 32;
     static constexpr int TILE = THREADS * IPT;
     static constexpr int IPW = 32 * IPT;
-    static constexpr size_t KEY_BYTES = size_t(TILE) * KB;
+    // +16: a tile starting off the 16-byte grid is copied from the aligned
+    // address below it and lands that many bytes into its region.
+    static constexpr size_t KEY_BYTES = size_t(TILE) * KB + 16;
     static constexpr size_t VAL_OFF = (KEY_BYTES + 127) & ~size_t(127);
-    static constexpr size_t BUF_BYTES = (VAL_OFF + size_t(TILE) * VB + 127) & ~size_t(127);
+    static constexpr size_t BUF_BYTES = (VAL_OFF + (VB ? size_t(TILE) * VB + 16 : 0) + 127) & ~size_t(127);
     static constexpr size_t HIST_OFF = 2 * BUF_BYTES;             // u32 [WARPS][256]
     static constexpr size_t GEXCL_OFF = HIST_OFF + size_t(WARPS) * 256 * 4;  // u64 [256]
     static constexpr size_t BINB_OFF = GEXCL_OFF + 256 * 8;       // u64 [256]
     static constexpr size_t SCAN64_OFF = BINB_OFF + 256 * 8;      // u64 [8]
     static constexpr size_t SCAN32_OFF = SCAN64_OFF + 64;         // u32 [8]
     static constexpr size_t MBAR_OFF = SCAN32_OFF + 64;           // u64 [2]
-    static constexpr size_t TILEID_OFF = MBAR_OFF + 16;           // u32 [2]
-    static constexpr size_t BINB32_OFF = TILEID_OFF + 16;         // u32 [256]
+    static constexpr size_t INFO_OFF = MBAR_OFF + 16;             // TileInfo [2]
+    static constexpr size_t BINB32_OFF = INFO_OFF + 2 * sizeof(TileInfo);  // u32 [256]
     static constexpr size_t MATCH_OFF = BINB32_OFF + 256 * 4;     // u32 [WARPS][256] when RANK_OR is used
     static constexpr size_t SMEM_BYTES = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);
     static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
-    static_assert(TILE % 16 == 0, "tile starts must stay 16-byte aligned");
+    static_assert(TILE % 16 == 0, "plain tiles start on the 16-byte grid");
 };
 
-template <int KB, int VB, class W, int THREADS, int IPT>
+// One onesweep digit pass.  SEG = false: one array of n keys.  SEG = true:
+// many independent segments; global tile g is p.tiles[g] (segment, base,
+// count), each segment's first tile publishes an inclusive prefix of its own
+// so lookback chains never cross segments, and digit bases come per segment
+// from p.seg_gofs.
+template <int KB, int VB, class W, int THREADS, int IPT, bool SEG>
 __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep_pass_kernel(PassParams p) {
     using U = typename KeyBits<KB>::U;
     using V = typename ValBits<VB>::V;
@@ -172,7 +191,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(smem + G::SCAN64_OFF);
     uint32_t* scan32 = reinterpret_cast<uint32_t*>(smem + G::SCAN32_OFF);
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + G::MBAR_OFF);
-    volatile uint32_t* tile_slot = reinterpret_cast<volatile uint32_t*>(smem + G::TILEID_OFF);
+    TileInfo* info_slot = reinterpret_cast<TileInfo*>(smem + G::INFO_OFF);
     uint32_t* binb32 = reinterpret_cast<uint32_t*>(smem + G::BINB32_OFF);
     uint32_t* match_scratch = reinterpret_cast<uint32_t*>(smem + G::MATCH_OFF);
     if constexpr (rank_uses_or(IPT)) {
@@ -193,69 +212,117 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         mbar_init(&mbar[1], 1);
         fence_mbar_init();
     }
-    {   // global exclusive digit offsets of this pass (once per CTA)
+    if constexpr (!SEG) {  // global exclusive digit offsets of this pass (once per CTA)
         const unsigned long long c = (tid < 256) ? p.gp_counts[tid] : 0ull;
         const unsigned long long ex = block_exclusive_scan_256<unsigned long long>(c, scan64, nullptr);
         if (tid < 256) gexcl[tid] = ex;
     }
 
-    // Thread 0 issues the bulk copies of a tile into buffer `slot`.
-    auto issue_tile = [&](uint32_t t, int slot) {
-        const uint64_t base = uint64_t(t) * G::TILE;
-        const uint64_t rem = n - base;
-        const uint32_t cnt = rem < uint64_t(G::TILE) ? uint32_t(rem) : uint32_t(G::TILE);
-        const uint32_t kb = p.tma_keys ? ((cnt * KB) & ~15u) : 0u;
-        const uint32_t vb = (PAIRS && p.tma_vals) ? ((cnt * VB) & ~15u) : 0u;
+    // Thread 0: describe tile t (its table entry `rec` in batched mode).
+    auto make_info = [&](uint32_t t, const TileRec& rec) {
+        TileInfo ti{};
+        ti.id = t;
+        if (t >= T) return ti;
+        if constexpr (SEG) {
+            ti.base = rec.base;
+            ti.cnt = rec.cnt;
+            ti.seg = rec.seg_flags >> 2;
+            ti.first = rec.seg_flags & 1u;
+            ti.last = (rec.seg_flags >> 1) & 1u;
+        } else {
+            ti.base = uint64_t(t) * G::TILE;
+            const uint64_t rem = n - ti.base;
+            ti.cnt = rem < uint64_t(G::TILE) ? uint32_t(rem) : uint32_t(G::TILE);
+            ti.first = t == 0;
+            ti.last = t + 1 == T;
+        }
+        return ti;
+    };
+    auto load_rec = [&](uint32_t t) {
+        TileRec r{};
+        if constexpr (SEG) {
+            if (t < T) r = p.tiles[t];
+        }
+        return r;
+    };
+    // Bulk copies of a tile into buffer `slot`, from the 16-byte-aligned
+    // address at or below the tile's start; the ragged tail (< 16 bytes) is
+    // left to plain loads.
+    auto issue_tile = [&](const TileInfo& ti, int slot) {
         uint8_t* buf = smem + size_t(slot) * G::BUF_BYTES;
-        mbar_arrive_expect_tx(&mbar[slot], kb + vb);
+        uint32_t kbytes = 0, vbytes = 0;
         const uint64_t pol = l2_evict_first_policy();
-        if (kb) bulk_copy_g2s(buf, gkeys_in + base, kb, &mbar[slot], pol);
-        if (PAIRS && vb) bulk_copy_g2s(buf + G::VAL_OFF, gvals_in + base, vb, &mbar[slot], pol);
+        const uintptr_t ka = reinterpret_cast<uintptr_t>(gkeys_in + ti.base);
+        const uint32_t mk = uint32_t(ka & 15u);
+        if (p.tma_keys) kbytes = (mk + ti.cnt * uint32_t(KB)) & ~15u;
+        uint32_t mv = 0;
+        uintptr_t va = 0;
+        if constexpr (PAIRS) {
+            va = reinterpret_cast<uintptr_t>(gvals_in + ti.base);
+            mv = uint32_t(va & 15u);
+            if (p.tma_vals) vbytes = (mv + ti.cnt * uint32_t(VB)) & ~15u;
+        }
+        mbar_arrive_expect_tx(&mbar[slot], kbytes + vbytes);
+        if (kbytes) bulk_copy_g2s(buf, reinterpret_cast<const void*>(ka - mk), kbytes, &mbar[slot], pol);
+        if (PAIRS && vbytes)
+            bulk_copy_g2s(buf + G::VAL_OFF, reinterpret_cast<const void*>(va - mv), vbytes, &mbar[slot], pol);
     };
 
-    // Tile ids come from the pass's atomic counter two tiles ahead (thread 0
-    // holds the id after next), so the atomic's latency hides behind a tile.
-    uint32_t id_after_next = 0;
+    // Tile ids come from the pass's atomic counter three tiles ahead: thread 0
+    // holds the next tile (being copied), the one after (its table entry
+    // loading) and the one after that (its id in flight), so neither the
+    // atomic's nor the table load's latency stalls a tile.
+    uint32_t id_an = 0, id_aan = 0;  // thread 0: ids of the tiles after next
+    TileRec rec_an{};                // thread 0: table entry of id_an
     __syncthreads();
     if (tid == 0) {
-        const uint32_t t = atomicAdd(p.tile_counter, 1u);
-        tile_slot[0] = t;
-        if (t < T) issue_tile(t, 0);
-        id_after_next = t < T ? atomicAdd(p.tile_counter, 1u) : T;
+        const uint32_t t0 = atomicAdd(p.tile_counter, 1u);
+        const TileInfo i0 = make_info(t0, load_rec(t0));
+        info_slot[0] = i0;
+        if (t0 < T) issue_tile(i0, 0);
+        id_an = t0 < T ? atomicAdd(p.tile_counter, 1u) : T;
+        rec_an = load_rec(id_an);
+        id_aan = id_an < T ? atomicAdd(p.tile_counter, 1u) : T;
     }
     __syncthreads();
-    uint32_t cur = tile_slot[0];
+    TileInfo cur = info_slot[0];
     uint32_t parity = 0;  // bit s: parity of the next wait on buffer s
     uint32_t it = 0;
 
     bool next_issued = false;  // thread 0 only: a copy into the other buffer is in flight
-    while (cur < T) {
+    while (cur.id < T) {
         const int b = int(it & 1u);
         if (tid == 0) {
-            const uint32_t nt = id_after_next;
-            tile_slot[(it + 1) & 1u] = nt;
-            next_issued = nt < T;
+            const TileInfo ni = make_info(id_an, rec_an);
+            info_slot[(it + 1) & 1u] = ni;
+            next_issued = ni.id < T;
             if (next_issued) {
                 fence_proxy_async_smem();
-                issue_tile(nt, b ^ 1);
-                id_after_next = atomicAdd(p.tile_counter, 1u);
+                issue_tile(ni, b ^ 1);
+                rec_an = load_rec(id_aan);
+                id_an = id_aan;
+                id_aan = id_aan < T ? atomicAdd(p.tile_counter, 1u) : T;
             }
+        }
+        unsigned long long seg_base_d = 0;  // batched: this tile's segment's digit base (bin owners)
+        if constexpr (SEG) {
+            if (tid < 256) seg_base_d = p.seg_gofs[size_t(cur.seg) * 256 + tid];
         }
         const bool landed = mbar_wait_bounded(&mbar[b], (parity >> b) & 1u, p.wait_limit_ns, p.err);
         parity ^= (1u << b);
 
-        const uint64_t tile_base = uint64_t(cur) * G::TILE;
-        const uint64_t rem = n - tile_base;
-        const uint32_t cnt = rem < uint64_t(G::TILE) ? uint32_t(rem) : uint32_t(G::TILE);
+        const uint32_t cnt = cur.cnt;
         const bool full = cnt == uint32_t(G::TILE);
         uint8_t* buf = smem + size_t(b) * G::BUF_BYTES;
-        U* sk = reinterpret_cast<U*>(buf);
+        U* sk = reinterpret_cast<U*>(buf);                 // staging (aligned)
         V* sv = reinterpret_cast<V*>(buf + G::VAL_OFF);
 
         // ---- load the tile into registers (warp-striped: stable rank order)
         U keys[IPT];
         V vals[PAIRS ? IPT : 1];
-        const bool fast = full && p.tma_keys && (!PAIRS || p.tma_vals);
+        const uint32_t mk = uint32_t(reinterpret_cast<uintptr_t>(gkeys_in + cur.base) & 15u);
+        const uint32_t mv = PAIRS ? uint32_t(reinterpret_cast<uintptr_t>(gvals_in + cur.base) & 15u) : 0u;
+        const bool fast = full && mk == 0 && mv == 0 && p.tma_keys && (!PAIRS || p.tma_vals);
         if (fast) {
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
@@ -264,14 +331,16 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
                 if constexpr (PAIRS) vals[u] = sv[j];
             }
         } else {
-            const uint32_t kb = p.tma_keys ? ((cnt * KB) & ~15u) : 0u;
-            const uint32_t vb = p.tma_vals ? ((cnt * VB) & ~15u) : 0u;
+            const uint32_t kbytes = p.tma_keys ? ((mk + cnt * uint32_t(KB)) & ~15u) : 0u;
+            const uint32_t vbytes = (PAIRS && p.tma_vals) ? ((mv + cnt * uint32_t(VB)) & ~15u) : 0u;
+            const U* ski = reinterpret_cast<const U*>(buf + mk);
+            const V* svi = reinterpret_cast<const V*>(buf + G::VAL_OFF + mv);
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
                 const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
                 if (j < cnt) {
-                    keys[u] = ((j + 1) * KB <= kb) ? sk[j] : gkeys_in[tile_base + j];
-                    if constexpr (PAIRS) vals[u] = ((j + 1) * VB <= vb) ? sv[j] : gvals_in[tile_base + j];
+                    keys[u] = (mk + (j + 1) * KB <= kbytes) ? ski[j] : gkeys_in[cur.base + j];
+                    if constexpr (PAIRS) vals[u] = (mv + (j + 1) * VB <= vbytes) ? svi[j] : gvals_in[cur.base + j];
                 } else {
                     keys[u] = U(~U(0));  // tail filler: sorts after every valid key
                 }
@@ -304,7 +373,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
             }
             return;
         }
-        const uint32_t next_tile = tile_slot[(it + 1) & 1u];
+        const TileInfo next_info = info_slot[(it + 1) & 1u];
 
         // ---- per-bin tile totals, warp bases, early PARTIAL publication
         uint32_t total = 0, valid_total = 0;
@@ -318,11 +387,11 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
                 total += c;
             }
             valid_total = total - ((tid == 255) ? (uint32_t(G::TILE) - cnt) : 0u);
-            st_relaxed(status + size_t(cur) * 256 + tid,
-                       Codec::pack(cur == 0 ? Codec::GLOBAL : Codec::PARTIAL, epoch, valid_total));
+            st_relaxed(status + size_t(cur.id) * 256 + tid,
+                       Codec::pack(cur.first ? Codec::GLOBAL : Codec::PARTIAL, epoch, valid_total));
 #if GBSORT_LOOKBACK_PREFETCH
             // first lookback round trip overlaps the scan and the rank
-            lookback_prefetch<LBW>(status, cur, tid, lb_pre);
+            if (!cur.first) lookback_prefetch<LBW>(status, cur.id, tid, lb_pre);
 #endif
         }
         const uint32_t excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
@@ -371,17 +440,18 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         // ---- decoupled lookback (bin owners), GLOBAL publication, bases
         if (tid < 256) {
             unsigned long long prefix = 0;
-            if (cur > 0) {
+            if (!cur.first) {
 #if GBSORT_LOOKBACK_PREFETCH
-                prefix = lookback_finish<Codec, LBW>(status, cur, tid, lb_pre, epoch, p.wait_limit_ns, p.err);
+                prefix = lookback_finish<Codec, LBW>(status, cur.id, tid, lb_pre, epoch, p.wait_limit_ns, p.err);
 #else
-                prefix = lookback_window<Codec, LBW>(status, cur, tid, epoch, p.wait_limit_ns, p.err);
+                prefix = lookback_window<Codec, LBW>(status, cur.id, tid, epoch, p.wait_limit_ns, p.err);
 #endif
-                if (cur + 1 < T)
-                    st_relaxed(status + size_t(cur) * 256 + tid,
+                if (!cur.last)
+                    st_relaxed(status + size_t(cur.id) * 256 + tid,
                                Codec::pack(Codec::GLOBAL, epoch, prefix + valid_total));
             }
-            const unsigned long long base = gexcl[tid] + prefix - excl;
+            const unsigned long long dbase = SEG ? seg_base_d : gexcl[tid];
+            const unsigned long long base = dbase + prefix - excl;
             binb[tid] = base;
             binb32[tid] = uint32_t(base);
         }
@@ -434,7 +504,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         }
         if (bad) atomicOr(p.err, ERRBIT_BOUNDS);
         __syncthreads();
-        cur = next_tile;
+        cur = next_info;
         ++it;
     }
 }

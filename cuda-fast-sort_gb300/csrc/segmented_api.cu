@@ -1,0 +1,533 @@
+// segmented_api.cu — batched (segmented) sort: plan, bind, graph-captured run,
+// size-bucket tuning table.  No reference counterpart (rsort sorts one array
+// per call); it builds on the same kernels as the plain sort.
+//
+// A plan classifies every segment by its size bucket (floor(log2 n)) into one
+// of three paths, per the tuning table:
+//   CTA_S    whole segment in one 256-thread CTA's shared memory
+//   CTA_L    whole segment in one 512-thread CTA's shared memory (bigger)
+//   ONESWEEP the segment's tiles join one global tile list; one upsweep, one
+//            scan, then one persistent launch per digit pass for all of them
+// Every launch pulls its work (chunk, segment or tile) from a device counter.
+// bind() uploads the tables into the caller's workspace once; run() captures
+// the launch sequence into a CUDA graph the first time and replays it after.
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gbsort.h"
+#include "plan.h"
+#include "device_common.cuh"
+#include "sort_params.h"
+
+namespace gbsort {
+
+const KernelEntry* seg_entries_k1();
+const KernelEntry* seg_entries_k2();
+const KernelEntry* seg_entries_k4();
+const KernelEntry* seg_entries_k8();
+const KernelEntry* seg_entries_k16();
+const KernelEntry* seg_upsweep_entry_k1();
+const KernelEntry* seg_upsweep_entry_k2();
+const KernelEntry* seg_upsweep_entry_k4();
+const KernelEntry* seg_upsweep_entry_k8();
+const KernelEntry* seg_upsweep_entry_k16();
+
+namespace {
+
+const KernelEntry* seg_entries(int kb) {
+    switch (kb) {
+        case 1: return seg_entries_k1();
+        case 2: return seg_entries_k2();
+        case 4: return seg_entries_k4();
+        case 8: return seg_entries_k8();
+        case 16: return seg_entries_k16();
+        default: return nullptr;
+    }
+}
+const KernelEntry* seg_upsweep_entry(int kb) {
+    switch (kb) {
+        case 1: return seg_upsweep_entry_k1();
+        case 2: return seg_upsweep_entry_k2();
+        case 4: return seg_upsweep_entry_k4();
+        case 8: return seg_upsweep_entry_k8();
+        case 16: return seg_upsweep_entry_k16();
+        default: return nullptr;
+    }
+}
+
+int width_index(int kb) { return kb == 1 ? 0 : kb == 2 ? 1 : kb == 4 ? 2 : kb == 8 ? 3 : 4; }
+
+constexpr uint64_t UPSWEEP_CHUNK = uint64_t(1) << 18;
+constexpr int BUCKETS = 41;  // floor(log2 n) = 0 .. 40
+
+// ---- tuning table: path per (key width, value size, size bucket) ---------
+std::mutex g_tune_mu;
+int g_tune[5][6][BUCKETS];
+bool g_tune_set[5][6];
+
+int path_for(int kb, int vb, uint64_t len, int s_max, int l_max) {
+    const int wi = width_index(kb), vi = value_index(vb);
+    int bucket = 0;
+    while (bucket + 1 < BUCKETS && (uint64_t(1) << (bucket + 1)) <= len) ++bucket;
+    int path = -1;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (g_tune_set[wi][vi]) path = g_tune[wi][vi][bucket];
+    }
+    if (path < 0) path = len <= uint64_t(s_max) ? GBSORT_PATH_CTA_S : len <= uint64_t(l_max) ? GBSORT_PATH_CTA_L
+                                                                                          : GBSORT_PATH_ONESWEEP;
+    // a path that cannot hold the segment falls through to the next one
+    if (path == GBSORT_PATH_CTA_S && len > uint64_t(s_max)) path = GBSORT_PATH_CTA_L;
+    if (path == GBSORT_PATH_CTA_L && len > uint64_t(l_max)) path = GBSORT_PATH_ONESWEEP;
+    return path;
+}
+
+// One CTA (256 threads) per (segment, pass): exclusive scan of the segment's
+// digit counts plus the segment's start = where each digit's run begins.
+__global__ void __launch_bounds__(256) seg_scan_kernel(SegScanParams p) {
+    __shared__ uint32_t tmp[16];
+    const uint32_t s = blockIdx.x / p.passes;
+    const uint32_t pp = blockIdx.x % p.passes;
+    const uint32_t c = p.seg_counts[(size_t(s) * p.passes + pp) * 256 + threadIdx.x];
+    const uint32_t excl = block_exclusive_scan_256<uint32_t>(c, tmp, nullptr);
+    p.seg_gofs[(size_t(pp) * p.segments + s) * 256 + threadIdx.x] = uint32_t(p.seg_begin[s]) + excl;
+}
+
+}  // namespace
+
+struct SegPlan {
+    int key_type = 0, kb = 0, vb = 0, kind = 0, passes = 0, desc = 0;
+    uint64_t n_total = 0;
+    size_t num_segments = 0;
+    KernelEntry pass{}, cta_s{}, cta_l{}, upsweep{};
+    std::vector<SegItem> small_s, small_l, up_items;
+    std::vector<unsigned long long> large_begin;
+    std::vector<TileRec> tiles;
+    uint64_t keys_in_cta = 0, keys_in_onesweep = 0;
+    // workspace layout
+    size_t alt_keys_off = 0, alt_vals_off = 0, ctl_off = 0, seg_counts_off = 0, zero_bytes = 0;
+    size_t seg_gofs_off = 0, seg_begin_off = 0, tiles_off = 0, up_items_off = 0, small_s_off = 0, small_l_off = 0;
+    size_t status_off = 0, status_bytes = 0, total_bytes = 0;
+    // ctl block: [0..15] tile counters, [16] upsweep items, [17] cta S, [18] cta L, [19] error word
+    // bound buffers and the cached graph
+    void* keys = nullptr;
+    void* vals = nullptr;
+    uint8_t* ws = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::mutex mu;
+};
+
+namespace {
+
+int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t* off, size_t num, SegPlan* p) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    const int vi = value_index(int(value_bytes));
+    if (kb == 0 || vi < 0 || value_bytes > 16 || (num > 0 && off == nullptr)) return GBSORT_ERR_INVALID_ARGUMENT;
+    p->key_type = key_type;
+    p->kb = int(kb);
+    p->vb = int(value_bytes);
+    p->kind = key_type >= GBSORT_KEY_F32 ? KIND_FLOAT : key_type >= GBSORT_KEY_I8 ? KIND_SIGNED : KIND_UNSIGNED;
+    p->passes = int(kb);
+    p->desc = descending ? 1 : 0;
+    p->num_segments = num;
+    const KernelEntry* se = seg_entries(p->kb) + vi * 3;
+    p->pass = se[0];
+    p->cta_s = se[1];
+    p->cta_l = se[2];
+    p->upsweep = *seg_upsweep_entry(p->kb);
+    int lg = 0;
+    while ((1 << (lg + 1)) <= p->passes) ++lg;
+    const uint64_t seg_value_limit = uint64_t(1) << (30 - lg);  // 32-bit status words
+    uint64_t n_total = 0;
+    for (size_t s = 0; s < num; ++s) {
+        if (off[s + 1] < off[s]) return GBSORT_ERR_INVALID_ARGUMENT;
+        n_total = std::max<uint64_t>(n_total, off[s + 1]);
+    }
+    if (n_total >= 0xFFFFFFFFull) {
+        set_last_error_text("segmented sort: the key array must hold fewer than 2^32 elements");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
+    p->n_total = n_total;
+    const uint64_t tile = uint64_t(p->pass.tile);
+    for (size_t s = 0; s < num; ++s) {
+        const uint64_t b = off[s], e = off[s + 1], len = e - b;
+        if (len <= 1) continue;  // already sorted
+        const int path = path_for(p->kb, p->vb, len, p->cta_s.tile, p->cta_l.tile);
+        SegItem it{b, e, 0, 0};
+        if (path == GBSORT_PATH_CTA_S) {
+            p->small_s.push_back(it);
+            p->keys_in_cta += len;
+        } else if (path == GBSORT_PATH_CTA_L) {
+            p->small_l.push_back(it);
+            p->keys_in_cta += len;
+        } else {
+            if (len > seg_value_limit) {
+                set_last_error_text("segmented sort: a segment exceeds the batched onesweep limit");
+                return GBSORT_ERR_INVALID_ARGUMENT;
+            }
+            const uint32_t idx = uint32_t(p->large_begin.size());
+            p->large_begin.push_back(b);
+            const uint64_t nt = (len + tile - 1) / tile;
+            for (uint64_t t = 0; t < nt; ++t) {
+                TileRec r{};
+                r.base = b + t * tile;
+                r.cnt = uint32_t(std::min<uint64_t>(tile, e - r.base));
+                r.seg_flags = (idx << 2) | (t + 1 == nt ? 2u : 0u) | (t == 0 ? 1u : 0u);
+                p->tiles.push_back(r);
+            }
+            for (uint64_t c = b; c < e; c += UPSWEEP_CHUNK)
+                p->up_items.push_back(SegItem{c, std::min<uint64_t>(e, c + UPSWEEP_CHUNK), idx, 0});
+            p->keys_in_onesweep += len;
+        }
+    }
+    if (p->tiles.size() >= 0xFFFFFFFFull) return GBSORT_ERR_INVALID_ARGUMENT;
+    // biggest segments first: better balance for the persistent CTA sorts
+    auto by_size = [](const SegItem& a, const SegItem& b) { return (a.end - a.begin) > (b.end - b.begin); };
+    std::stable_sort(p->small_s.begin(), p->small_s.end(), by_size);
+    std::stable_sort(p->small_l.begin(), p->small_l.end(), by_size);
+    std::stable_sort(p->up_items.begin(), p->up_items.end(), by_size);
+
+    const size_t L = p->large_begin.size();
+    size_t o = 0;
+    p->alt_keys_off = o;
+    o = align_up(o + (L ? size_t(n_total) * kb : 0), 256);
+    p->alt_vals_off = o;
+    o = align_up(o + (L ? size_t(n_total) * value_bytes : 0), 256);
+    p->ctl_off = o;
+    o = align_up(o + 256, 256);
+    p->seg_counts_off = o;
+    o = align_up(o + L * p->passes * 256 * 4, 256);
+    p->zero_bytes = o - p->ctl_off;
+    p->seg_gofs_off = o;
+    o = align_up(o + L * p->passes * 256 * 4, 256);
+    p->seg_begin_off = o;
+    o = align_up(o + L * 8, 256);
+    p->tiles_off = o;
+    o = align_up(o + p->tiles.size() * sizeof(TileRec), 256);
+    p->up_items_off = o;
+    o = align_up(o + p->up_items.size() * sizeof(SegItem), 256);
+    p->small_s_off = o;
+    o = align_up(o + p->small_s.size() * sizeof(SegItem), 256);
+    p->small_l_off = o;
+    o = align_up(o + p->small_l.size() * sizeof(SegItem), 256);
+    p->status_off = o;
+    p->status_bytes = p->tiles.size() * 256 * 4;
+    o = align_up(o + p->status_bytes, 256);
+    p->total_bytes = o;
+    return GBSORT_OK;
+}
+
+int launch(const KernelEntry& e, uint32_t grid, void* params, cudaStream_t s, const char* what) {
+    void* args[] = {params};
+    const cudaError_t err = cudaLaunchKernel(e.fn, dim3(grid), dim3(e.threads), args, e.smem, s);
+    if (err != cudaSuccess) {
+        set_last_error(what, err);
+        return GBSORT_ERR_CUDA;
+    }
+    return GBSORT_OK;
+}
+
+uint32_t grid_for(const KernelEntry& e, uint64_t work) {
+    const uint64_t cap = uint64_t(device_sm_count()) * uint64_t(std::max(1, resident_ctas(e)));
+    return uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(cap, work)));
+}
+
+int enqueue_segmented(SegPlan* p, cudaStream_t s) {
+    uint8_t* ws = p->ws;
+    uint32_t* ctl = reinterpret_cast<uint32_t*>(ws + p->ctl_off);
+    uint32_t* err = ctl + 19;
+    cudaError_t e = cudaMemsetAsync(ws + p->ctl_off, 0, p->zero_bytes, s);
+    if (e != cudaSuccess) {
+        set_last_error("segmented memset", e);
+        return GBSORT_ERR_CUDA;
+    }
+    const size_t L = p->large_begin.size();
+    const bool odd = (p->passes & 1) != 0;
+    void* alt_keys = ws + p->alt_keys_off;
+    void* alt_vals = p->vb ? ws + p->alt_vals_off : nullptr;
+    int st;
+    if (L) {
+        SegUpsweepParams up{};
+        up.keys = p->keys;
+        up.kind = p->kind;
+        up.desc = p->desc;
+        up.items = reinterpret_cast<const SegItem*>(ws + p->up_items_off);
+        up.num_items = uint32_t(p->up_items.size());
+        up.item_counter = ctl + 16;
+        up.seg_counts = reinterpret_cast<uint32_t*>(ws + p->seg_counts_off);
+        up.status = ws + p->status_off;
+        up.status_bytes = p->status_bytes;
+        up.mirror_keys = odd ? alt_keys : nullptr;
+        up.vals = p->vals;
+        up.mirror_vals = (odd && p->vb) ? alt_vals : nullptr;
+        up.val_bytes = uint32_t(p->vb);
+        if ((st = launch(p->upsweep, grid_for(p->upsweep, p->up_items.size()), &up, s, "segmented upsweep")))
+            return st;
+        SegScanParams sc{};
+        sc.seg_counts = up.seg_counts;
+        sc.seg_begin = reinterpret_cast<const unsigned long long*>(ws + p->seg_begin_off);
+        sc.seg_gofs = reinterpret_cast<uint32_t*>(ws + p->seg_gofs_off);
+        sc.segments = uint32_t(L);
+        sc.passes = uint32_t(p->passes);
+        void* args[] = {&sc};
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(&seg_scan_kernel), dim3(uint32_t(L) * p->passes),
+                             dim3(256), args, 0, s);
+        if (e != cudaSuccess) {
+            set_last_error("segmented scan", e);
+            return GBSORT_ERR_CUDA;
+        }
+    }
+    auto cta_launch = [&](const KernelEntry& k, const std::vector<SegItem>& v, size_t off, int ctr) {
+        if (v.empty()) return int(GBSORT_OK);
+        CtaSortParams cp{};
+        cp.keys = p->keys;
+        cp.vals = p->vals;
+        cp.segs = reinterpret_cast<const SegItem*>(ws + off);
+        cp.num_segs = uint32_t(v.size());
+        cp.seg_counter = ctl + ctr;
+        cp.kind = p->kind;
+        cp.desc = p->desc;
+        cp.passes = p->passes;
+        return launch(k, grid_for(k, v.size()), &cp, s, "segmented CTA sort");
+    };
+    if ((st = cta_launch(p->cta_l, p->small_l, p->small_l_off, 18))) return st;
+    if ((st = cta_launch(p->cta_s, p->small_s, p->small_s_off, 17))) return st;
+    if (L) {
+        const uint32_t T = uint32_t(p->tiles.size());
+        const uint32_t grid = grid_for(p->pass, T);
+        for (int pass = 0; pass < p->passes; ++pass) {
+            const bool from_user = ((pass + (odd ? 1 : 0)) & 1) == 0;
+            PassParams pp{};
+            pp.keys_in = from_user ? p->keys : alt_keys;
+            pp.keys_out = from_user ? alt_keys : p->keys;
+            pp.vals_in = p->vb ? (from_user ? p->vals : alt_vals) : nullptr;
+            pp.vals_out = p->vb ? (from_user ? alt_vals : p->vals) : nullptr;
+            pp.n = p->n_total;
+            pp.num_tiles = T;
+            pp.pass = pass;
+            pp.kind = p->kind;
+            pp.desc = p->desc;
+            pp.twiddle_load = pass == 0;
+            pp.twiddle_store = pass == p->passes - 1;
+            pp.tma_keys = 1;
+            pp.tma_vals = p->vb ? 1 : 0;
+            pp.gp_counts = nullptr;
+            pp.status = ws + p->status_off;
+            pp.tile_counter = ctl + pass;
+            pp.err = err;
+            pp.wait_limit_ns = wait_limit_ns();
+            pp.tiles = reinterpret_cast<const TileRec*>(ws + p->tiles_off);
+            pp.seg_gofs = reinterpret_cast<const uint32_t*>(ws + p->seg_gofs_off) + size_t(pass) * L * 256;
+            if ((st = launch(p->pass, grid, &pp, s, "segmented pass"))) return st;
+        }
+    }
+    return GBSORT_OK;
+}
+
+int prepare_all(SegPlan* p) {
+    int st;
+    if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
+    if (!p->large_begin.empty()) {
+        if ((st = prepare_kernel(p->pass))) return st;
+        if ((st = prepare_kernel(p->upsweep))) return st;
+    }
+    if (!p->small_s.empty() && (st = prepare_kernel(p->cta_s))) return st;
+    if (!p->small_l.empty() && (st = prepare_kernel(p->cta_l))) return st;
+    return GBSORT_OK;
+}
+
+void drop_graph(SegPlan* p) {
+    if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+}
+
+}  // namespace
+}  // namespace gbsort
+
+using namespace gbsort;
+
+struct gbsort_segmented_plan : SegPlan {};
+
+extern "C" {
+
+int gbsort_segmented_plan_create(int key_type, size_t value_bytes, int descending, const uint64_t* h_offsets,
+                                 size_t num_segments, gbsort_segmented_plan** out) {
+    if (out == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    auto* p = new gbsort_segmented_plan();
+    const int st = build_plan(key_type, value_bytes, descending, h_offsets, num_segments, p);
+    if (st != GBSORT_OK) {
+        delete p;
+        return st;
+    }
+    *out = p;
+    return GBSORT_OK;
+}
+
+void gbsort_segmented_plan_destroy(gbsort_segmented_plan* plan) {
+    if (!plan) return;
+    drop_graph(plan);
+    delete plan;
+}
+
+int gbsort_segmented_plan_info(const gbsort_segmented_plan* p, gbsort_segmented_info* out) {
+    if (!p || !out) return GBSORT_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    out->num_segments = p->num_segments;
+    out->cta_small_segments = p->small_s.size();
+    out->cta_large_segments = p->small_l.size();
+    out->onesweep_segments = p->large_begin.size();
+    out->onesweep_tiles = p->tiles.size();
+    out->keys_in_cta = p->keys_in_cta;
+    out->keys_in_onesweep = p->keys_in_onesweep;
+    out->cta_small_max = uint32_t(p->cta_s.tile);
+    out->cta_large_max = uint32_t(p->cta_l.tile);
+    out->onesweep_tile = uint32_t(p->pass.tile);
+    out->workspace_bytes = p->total_bytes;
+    return GBSORT_OK;
+}
+
+int gbsort_segmented_bind(gbsort_segmented_plan* p, void* d_keys, void* d_values, void* d_workspace,
+                          size_t workspace_bytes, void* stream) {
+    if (!p || (p->num_segments && !d_keys) || (p->vb && p->num_segments && !d_values)) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (d_workspace == nullptr || workspace_bytes < p->total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    if ((reinterpret_cast<uintptr_t>(d_keys) % p->kb) || (p->vb && reinterpret_cast<uintptr_t>(d_values) % p->vb))
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(p->mu);
+    const int st = prepare_all(p);
+    if (st != GBSORT_OK) return st;
+    if (p->keys != d_keys || p->vals != d_values || p->ws != d_workspace) drop_graph(p);
+    p->keys = d_keys;
+    p->vals = d_values;
+    p->ws = static_cast<uint8_t*>(d_workspace);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    auto up = [&](size_t off, const void* src, size_t bytes) {
+        return bytes ? cudaMemcpyAsync(p->ws + off, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    };
+    cudaError_t e = up(p->tiles_off, p->tiles.data(), p->tiles.size() * sizeof(TileRec));
+    if (e == cudaSuccess) e = up(p->up_items_off, p->up_items.data(), p->up_items.size() * sizeof(SegItem));
+    if (e == cudaSuccess) e = up(p->small_s_off, p->small_s.data(), p->small_s.size() * sizeof(SegItem));
+    if (e == cudaSuccess) e = up(p->small_l_off, p->small_l.data(), p->small_l.size() * sizeof(SegItem));
+    if (e == cudaSuccess) e = up(p->seg_begin_off, p->large_begin.data(), p->large_begin.size() * 8);
+    if (e != cudaSuccess) {
+        set_last_error("segmented table upload", e);
+        return GBSORT_ERR_CUDA;
+    }
+    return GBSORT_OK;
+}
+
+// Runs the bound plan.  use_graph != 0: the first run captures the launch
+// sequence into a CUDA graph (the stream must be capturable: not the legacy
+// default stream) and later runs replay it; 0: plain launches every time.
+int gbsort_segmented_run(gbsort_segmented_plan* p, int use_graph, void* stream) {
+    if (!p || !p->ws) return GBSORT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(p->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!use_graph || s == nullptr) return enqueue_segmented(p, s);
+    if (!p->exec) {
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            set_last_error("segmented graph capture", e);
+            return GBSORT_ERR_CUDA;
+        }
+        const int st = enqueue_segmented(p, s);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(s, &g);
+        if (st != GBSORT_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) set_last_error("segmented graph capture", e);
+            return st != GBSORT_OK ? st : GBSORT_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&p->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            p->exec = nullptr;
+            set_last_error("segmented graph instantiate", e);
+            return GBSORT_ERR_CUDA;
+        }
+    }
+    const cudaError_t e = cudaGraphLaunch(p->exec, s);
+    if (e != cudaSuccess) {
+        set_last_error("segmented graph launch", e);
+        return GBSORT_ERR_CUDA;
+    }
+    return GBSORT_OK;
+}
+
+int gbsort_segmented_status(gbsort_segmented_plan* p, void* stream) {
+    if (!p || !p->ws) return GBSORT_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    uint32_t err = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&err, p->ws + p->ctl_off + 19 * 4, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_last_error("segmented status", e);
+        return GBSORT_ERR_CUDA;
+    }
+    if (err & ERRBIT_BOUNDS) return GBSORT_ERR_INTERNAL;
+    if (err & ERRBIT_TIMEOUT) return GBSORT_ERR_TIMEOUT;
+    return GBSORT_OK;
+}
+
+int gbsort_segmented_sort(int key_type, int descending, void* d_keys, void* d_values, size_t value_bytes,
+                          const uint64_t* h_offsets, size_t num_segments, size_t* temp_bytes, void* d_workspace,
+                          void* stream) {
+    if (temp_bytes == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    gbsort_segmented_plan* p = nullptr;
+    int st = gbsort_segmented_plan_create(key_type, value_bytes, descending, h_offsets, num_segments, &p);
+    if (st != GBSORT_OK) return st;
+    if (d_workspace == nullptr) {
+        *temp_bytes = p->total_bytes;
+        gbsort_segmented_plan_destroy(p);
+        return GBSORT_OK;
+    }
+    st = gbsort_segmented_bind(p, d_keys, d_values, d_workspace, *temp_bytes, stream);
+    if (st == GBSORT_OK) st = gbsort_segmented_run(p, 0, stream);
+    // the tables were uploaded from the plan's host memory: keep it alive
+    // until the copies have been consumed
+    if (st == GBSORT_OK) {
+        const cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) {
+            set_last_error("segmented sort", e);
+            st = GBSORT_ERR_CUDA;
+        }
+    }
+    gbsort_segmented_plan_destroy(p);
+    return st;
+}
+
+int gbsort_set_segmented_path(int key_type, size_t value_bytes, int size_log2, int path) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    const int vi = value_index(int(value_bytes));
+    if (kb == 0 || vi < 0 || size_log2 < -1 || size_log2 >= BUCKETS || path < -1 || path > GBSORT_PATH_ONESWEEP)
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const int wi = width_index(int(kb));
+    if (!g_tune_set[wi][vi]) {
+        for (int b = 0; b < BUCKETS; ++b) g_tune[wi][vi][b] = -1;
+        g_tune_set[wi][vi] = true;
+    }
+    if (size_log2 < 0) {
+        for (int b = 0; b < BUCKETS; ++b) g_tune[wi][vi][b] = path;
+    } else {
+        g_tune[wi][vi][size_log2] = path;
+    }
+    return GBSORT_OK;
+}
+
+int gbsort_get_segmented_path(int key_type, size_t value_bytes, int size_log2) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    const int vi = value_index(int(value_bytes));
+    if (kb == 0 || vi < 0 || size_log2 < 0 || size_log2 >= BUCKETS) return -2;
+    const uint64_t len = uint64_t(1) << size_log2;
+    const KernelEntry* se = seg_entries(int(kb)) + vi * 3;
+    return path_for(int(kb), int(value_bytes), len, se[1].tile, se[2].tile);
+}
+
+}  // extern "C"

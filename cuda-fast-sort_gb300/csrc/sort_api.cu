@@ -291,8 +291,9 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         pp.desc = descending;
         pp.twiddle_load = pass == 0;
         pp.twiddle_store = pass == plan.passes - 1;
-        pp.tma_keys = (reinterpret_cast<uintptr_t>(pp.keys_in) & 15) == 0;
-        pp.tma_vals = plan.vb ? ((reinterpret_cast<uintptr_t>(pp.vals_in) & 15) == 0) : 0;
+        // bulk copies start at the 16-byte boundary at or below each tile
+        pp.tma_keys = 1;
+        pp.tma_vals = plan.vb ? 1 : 0;
         pp.gp_counts = gp + size_t(pass) * 256;
         pp.status = status;
         pp.tile_counter = counters + pass;
@@ -325,6 +326,10 @@ using namespace gbsort;
 
 namespace {
 
+bool naturally_aligned(const void* p, size_t bytes) {
+    return p == nullptr || bytes == 0 || (reinterpret_cast<uintptr_t>(p) % bytes) == 0;
+}
+
 int status_from_error_word(uint32_t err) {
     if (err & ERRBIT_BOUNDS) return GBSORT_ERR_INTERNAL;
     if (err & ERRBIT_TIMEOUT) return GBSORT_ERR_TIMEOUT;
@@ -353,6 +358,10 @@ int sort_common(int key_type, int descending, void* d_keys, void* d_values, size
     }
     if (n == 0) return GBSORT_OK;
     if (d_keys == nullptr || (value_bytes != 0 && d_values == nullptr)) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (!naturally_aligned(d_keys, size_t(plan.kb)) || !naturally_aligned(d_values, value_bytes)) {
+        set_last_error_text("keys and values must be aligned to their own size");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
     if (*temp_bytes < plan.total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
     return enqueue_sort(plan, descending ? 1 : 0, d_keys, d_values, d_workspace,
                         static_cast<cudaStream_t>(stream), nullptr, 0, nullptr);

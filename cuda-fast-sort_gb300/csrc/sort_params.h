@@ -22,6 +22,13 @@ struct HistParams {
     uint64_t val_bytes_total;   // n * value bytes
 };
 
+// Batched mode: one entry per global tile, built on the host.
+struct alignas(16) TileRec {
+    unsigned long long base;  // index of the tile's first element in the key array
+    uint32_t cnt;             // elements in the tile
+    uint32_t seg_flags;       // segment << 2 | last << 1 | first
+};
+
 // One onesweep digit pass (one persistent launch per digit).
 struct PassParams {
     const void* keys_in;
@@ -42,6 +49,54 @@ struct PassParams {
     uint32_t* tile_counter;     // this pass's dynamic tile counter (zeroed)
     uint32_t* err;              // workspace error word
     uint64_t wait_limit_ns;
+    // batched mode only
+    const TileRec* tiles;       // [num_tiles]
+    const uint32_t* seg_gofs;   // [segments][256] absolute output base of each digit, this pass
+};
+
+// Batched upsweep: one work item per chunk of one segment.
+struct SegItem {
+    unsigned long long begin, end;  // element range (within one segment)
+    uint32_t seg;                   // onesweep segment index
+    uint32_t pad;
+};
+
+struct SegUpsweepParams {
+    const void* keys;
+    int kind;
+    int desc;
+    const SegItem* items;
+    uint32_t num_items;
+    uint32_t* item_counter;     // zeroed
+    uint32_t* seg_counts;       // [segments][passes][256], zeroed
+    void* status;               // lookback status array to clear
+    uint64_t status_bytes;
+    // odd pass counts: mirror each item's keys/values into the alternate buffer
+    void* mirror_keys;
+    const void* vals;
+    void* mirror_vals;
+    uint32_t val_bytes;
+};
+
+// Batched: digit counts -> absolute digit bases, one CTA per (segment, pass).
+struct SegScanParams {
+    const uint32_t* seg_counts;           // [segments][passes][256]
+    const unsigned long long* seg_begin;  // [segments]
+    uint32_t* seg_gofs;                   // [passes][segments][256]
+    uint32_t segments;
+    uint32_t passes;
+};
+
+// Small segments sorted whole inside one CTA's shared memory.
+struct CtaSortParams {
+    void* keys;
+    void* vals;
+    const SegItem* segs;        // [num_segs] (begin, end)
+    uint32_t num_segs;
+    uint32_t* seg_counter;      // zeroed
+    int kind;
+    int desc;
+    int passes;
 };
 
 }  // namespace gbsort

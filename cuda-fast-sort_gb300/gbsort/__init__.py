@@ -59,6 +59,19 @@ class PlanInfo(ctypes.Structure):
     ]
 
 
+class SegmentedInfo(ctypes.Structure):
+    _fields_ = [
+        ("num_segments", ctypes.c_uint64), ("cta_small_segments", ctypes.c_uint64),
+        ("cta_large_segments", ctypes.c_uint64), ("onesweep_segments", ctypes.c_uint64),
+        ("onesweep_tiles", ctypes.c_uint64), ("keys_in_cta", ctypes.c_uint64),
+        ("keys_in_onesweep", ctypes.c_uint64), ("cta_small_max", ctypes.c_uint32),
+        ("cta_large_max", ctypes.c_uint32), ("onesweep_tile", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+        ("workspace_bytes", ctypes.c_uint64),
+    ]
+
+
+PATH_CTA_S, PATH_CTA_L, PATH_ONESWEEP = 0, 1, 2
+
 _lib = None
 
 
@@ -84,6 +97,18 @@ def _declare(lib: ctypes.CDLL) -> None:
         "gbsort_generate": (i, [i, sz, vp, sz, u64, vp]),
         "gbsort_device_sm_count": (i, []),
     }
+    pplan = ctypes.POINTER(ctypes.c_void_p)
+    sig.update({
+        "gbsort_segmented_plan_create": (i, [i, sz, i, ctypes.POINTER(ctypes.c_uint64), sz, pplan]),
+        "gbsort_segmented_plan_destroy": (None, [vp]),
+        "gbsort_segmented_plan_info": (i, [vp, ctypes.POINTER(SegmentedInfo)]),
+        "gbsort_segmented_bind": (i, [vp, vp, vp, vp, sz, vp]),
+        "gbsort_segmented_run": (i, [vp, i, vp]),
+        "gbsort_segmented_status": (i, [vp, vp]),
+        "gbsort_segmented_sort": (i, [i, i, vp, vp, sz, ctypes.POINTER(ctypes.c_uint64), sz, psz, vp, vp]),
+        "gbsort_set_segmented_path": (i, [i, sz, i, i]),
+        "gbsort_get_segmented_path": (i, [i, sz, i]),
+    })
     for name in TYPED_NAMES:
         sig[f"gbsort_sort_{name}"] = (i, [vp, psz, vp, sz, vp])
         sig[f"gbsort_sort_{name}_desc"] = (i, [vp, psz, vp, sz, vp])
@@ -236,3 +261,77 @@ def probe_wait_timeout(scratch, limit_ns: int, stream=None) -> int:
 
 def sm_count() -> int:
     return lib().gbsort_device_sm_count()
+
+
+# ---- batched (segmented) sort ---------------------------------------------
+
+def _offsets_array(offsets):
+    import numpy as np
+
+    off = np.ascontiguousarray(np.asarray(offsets, dtype=np.uint64))
+    return off, off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+
+
+class SegmentedPlan:
+    """A batched sort of many independent segments (offsets on the host).
+    bind() device buffers + workspace once, run() as often as needed (the
+    first graph run captures a CUDA graph that later runs replay)."""
+
+    def __init__(self, key_type, offsets, value_bytes: int = 0, descending: bool = False):
+        self._off, ptr = _offsets_array(offsets)
+        h = ctypes.c_void_p()
+        _check(lib().gbsort_segmented_plan_create(key_type_id(key_type), value_bytes, int(descending), ptr,
+                                                  len(self._off) - 1, ctypes.byref(h)), "segmented plan")
+        self.handle = h
+        self.key_type = key_type
+        self.value_bytes = value_bytes
+
+    def info(self) -> dict:
+        inf = SegmentedInfo()
+        _check(lib().gbsort_segmented_plan_info(self.handle, ctypes.byref(inf)), "segmented info")
+        return {f: getattr(inf, f) for f, _ in SegmentedInfo._fields_ if f != "pad"}
+
+    @property
+    def workspace_bytes(self) -> int:
+        return self.info()["workspace_bytes"]
+
+    def bind(self, keys, workspace, workspace_bytes: int, values=None, stream=None) -> None:
+        _check(lib().gbsort_segmented_bind(self.handle, _ptr(keys), _ptr(values), _ptr(workspace), workspace_bytes,
+                                           _stream(stream)), "segmented bind")
+
+    def run(self, stream=None, use_graph: bool = True) -> None:
+        _check(lib().gbsort_segmented_run(self.handle, int(use_graph), _stream(stream)), "segmented run")
+
+    def status(self, stream=None) -> int:
+        return lib().gbsort_segmented_status(self.handle, _stream(stream))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().gbsort_segmented_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def segmented_sort(keys, key_type, offsets, workspace=None, workspace_bytes: int = 0, values=None,
+                   value_bytes: int = 0, descending: bool = False, stream=None) -> int:
+    """One-shot batched sort (rsort-style size query when workspace is None:
+    returns the bytes needed)."""
+    off, ptr = _offsets_array(offsets)
+    tb = ctypes.c_size_t(workspace_bytes)
+    st = lib().gbsort_segmented_sort(key_type_id(key_type), int(descending), _ptr(keys), _ptr(values), value_bytes,
+                                     ptr, len(off) - 1, ctypes.byref(tb), _ptr(workspace), _stream(stream))
+    _check(st, "segmented sort")
+    return tb.value
+
+
+def set_segmented_path(key_type, value_bytes: int, size_log2: int, path: int) -> None:
+    _check(lib().gbsort_set_segmented_path(key_type_id(key_type), value_bytes, size_log2, path), "tuning")
+
+
+def get_segmented_path(key_type, value_bytes: int, size_log2: int) -> int:
+    return lib().gbsort_get_segmented_path(key_type_id(key_type), value_bytes, size_log2)

@@ -157,6 +157,75 @@ int gbsort_sort_host(int key_type, int descending, void* h_keys,
                      void* d_buffer, size_t buffer_bytes, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched (segmented) sort — no counterpart in the reference (one array per */
+/* rsort call).  Thousands of independent sorts of uneven sizes run in a     */
+/* few persistent launches: small segments sorted whole in one CTA's shared  */
+/* memory, large ones through onesweep passes over one global tile list.     */
+/* Segment i is elements [offsets[i], offsets[i+1]) of the key (and value)   */
+/* arrays; the arrays must hold fewer than 2^32 elements.                    */
+/* ------------------------------------------------------------------------ */
+
+/* Paths a size bucket can take (see gbsort_set_segmented_path). */
+enum {
+    GBSORT_PATH_CTA_S = 0,    /* whole segment in a 256-thread CTA          */
+    GBSORT_PATH_CTA_L = 1,    /* whole segment in a 512-thread CTA          */
+    GBSORT_PATH_ONESWEEP = 2  /* onesweep passes over the global tile list  */
+};
+
+typedef struct gbsort_segmented_plan gbsort_segmented_plan;
+
+typedef struct gbsort_segmented_info {
+    uint64_t num_segments;
+    uint64_t cta_small_segments;
+    uint64_t cta_large_segments;
+    uint64_t onesweep_segments;
+    uint64_t onesweep_tiles;
+    uint64_t keys_in_cta;
+    uint64_t keys_in_onesweep;
+    uint32_t cta_small_max;   /* largest segment the 256-thread CTA sort takes */
+    uint32_t cta_large_max;   /* largest segment the 512-thread CTA sort takes */
+    uint32_t onesweep_tile;   /* keys per onesweep tile                        */
+    uint32_t pad;
+    uint64_t workspace_bytes;
+} gbsort_segmented_info;
+
+/* Plan from HOST offsets (num_segments + 1 entries, non-decreasing). */
+int gbsort_segmented_plan_create(int key_type, size_t value_bytes,
+                                 int descending, const uint64_t* h_offsets,
+                                 size_t num_segments,
+                                 gbsort_segmented_plan** out);
+void gbsort_segmented_plan_destroy(gbsort_segmented_plan* plan);
+int gbsort_segmented_plan_info(const gbsort_segmented_plan* plan,
+                               gbsort_segmented_info* out);
+/* Bind device keys/values and a workspace of >= info.workspace_bytes; uploads
+ * the plan's tables into the workspace on `stream`. */
+int gbsort_segmented_bind(gbsort_segmented_plan* plan, void* d_keys,
+                          void* d_values, void* d_workspace,
+                          size_t workspace_bytes, void* stream);
+/* Sort every segment in place.  use_graph: the first run captures the launch
+ * sequence into a CUDA graph on `stream` (must not be the legacy default
+ * stream), later runs replay it; rebinding other buffers drops the graph. */
+int gbsort_segmented_run(gbsort_segmented_plan* plan, int use_graph,
+                         void* stream);
+/* Synchronizes `stream` and reads the plan's device error word. */
+int gbsort_segmented_status(gbsort_segmented_plan* plan, void* stream);
+/* One-shot form with rsort's protocol: d_workspace == NULL writes the bytes
+ * needed to *temp_bytes.  Synchronizes `stream` before returning. */
+int gbsort_segmented_sort(int key_type, int descending, void* d_keys,
+                          void* d_values, size_t value_bytes,
+                          const uint64_t* h_offsets, size_t num_segments,
+                          size_t* temp_bytes, void* d_workspace, void* stream);
+/* Tuning table: the path segments of size [2^size_log2, 2^(size_log2+1))
+ * take for this key type and value size (size_log2 = -1: every bucket;
+ * path = -1: back to the built-in size thresholds).  A path too small for a
+ * segment falls through to the next bigger one.  Plans made afterwards use
+ * it. */
+int gbsort_set_segmented_path(int key_type, size_t value_bytes, int size_log2,
+                              int path);
+/* Path a segment of exactly 2^size_log2 keys would take now. */
+int gbsort_get_segmented_path(int key_type, size_t value_bytes, int size_log2);
+
+/* ------------------------------------------------------------------------ */
 /* Workspace status and bounded waits                                       */
 /* ------------------------------------------------------------------------ */
 
