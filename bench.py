@@ -58,6 +58,9 @@ CONFIGS = {
                 workload="u64 keys (upper 32 bits from 256 values) + u64 index values, n=2^27, descending"),
     "c3b": dict(key="u128", n=1 << 26, dist=0, vb=0, desc=True,
                 workload="u128 keys (two uniform 64-bit halves), keys-only, n=2^26, descending"),
+    "c4": dict(key="u32", n=0, dist=0, vb=4, desc=False, segments=4096, seg_log2=(8, 20),
+               workload="batched: 4096 independent u32-key/u32-value sorts, segment lengths log-uniform in "
+                        "[2^8, 2^20] (seeded), keys uniform 32-bit, ascending, one batched run per step"),
 }
 KEY_BYTES = {"u32": 4, "f32": 4, "u64": 8, "u128": 16}
 FALLBACK_HBM_GBS = 6800.0
@@ -201,13 +204,14 @@ def bench_reference(args, cfg, world, rank):
 
     oracle = _oracle.load()
     # size the per-step sample so the whole run stays within ~2 minutes
-    probe_n = min(cfg["n"], 1 << 22)
+    n_cfg = cfg["n"] or (1 << 29)  # batched: the workload's total keys
+    probe_n = min(n_cfg, 1 << 22)
     probe = cpu_sample_bits(cfg, probe_n, seed=6)
     t0 = time.perf_counter()
     oracle.sort(cfg["key"], probe, cfg["desc"], None, threads=cores)
     per_key = (time.perf_counter() - t0) / probe_n * (2.0 if cfg["vb"] else 1.0)
     budget = 120.0 / max(1, args.steps + args.warmup)
-    n_sample = int(min(cfg["n"], 1 << 26, max(1 << 20, budget / max(per_key, 1e-12))))
+    n_sample = int(min(n_cfg, 1 << 26, max(1 << 20, budget / max(per_key, 1e-12))))
     raw = cpu_sample_bits(cfg, n_sample, seed=7)
     vals = np.arange(n_sample, dtype=np.uint32 if cfg["vb"] == 4 else np.uint64) if cfg["vb"] else None
     for _ in range(args.warmup):
@@ -426,6 +430,132 @@ def bench_gbsort(args, cfg, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def bench_batched(args, cfg, world, rank, local):
+    """Batched segmented sort vs looping the plain sort over the same segments."""
+    import numpy as np
+    import torch
+
+    import gbsort
+    from gbsort import gen
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    kt, vb = cfg["key"], cfg["vb"]
+    sizes = gen.log_uniform_sizes(cfg["segments"], cfg["seg_log2"][0], cfg["seg_log2"][1], seed=2026 + rank)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    n = int(off[-1])
+    keys = torch.empty(n, dtype=torch.int32, device=dev)
+    vals = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    # autotune the size buckets of this workload (not timed)
+    scratch_bytes = (4 + vb) * (24 << 20) + (64 << 20)
+    scratch = torch.empty(scratch_bytes, dtype=torch.uint8, device=dev)
+    t0 = time.time()
+    report = gbsort.autotune_segmented(kt, vb, scratch, scratch_bytes, cfg["seg_log2"][0], cfg["seg_log2"][1],
+                                       stream=stream)
+    tune_s = time.time() - t0
+    del scratch
+
+    plan = gbsort.SegmentedPlan(kt, off, vb)
+    info = plan.info()
+    ws = torch.empty(info["workspace_bytes"], dtype=torch.uint8, device=dev)
+    plan.bind(keys, ws, info["workspace_bytes"], values=vals, stream=stream)
+
+    def prepare(seed):
+        with torch.cuda.stream(stream):
+            gbsort.generate(0, 4, keys, n, seed, stream)
+            gbsort.generate(3, 4, vals, n, 0, stream)  # value = index
+            flush.fill_(seed & 0xFF)
+
+    for w in range(args.warmup):
+        prepare(10 + w)
+        plan.run(stream=stream)
+    if plan.status(stream=stream) != gbsort.OK:
+        raise RuntimeError("batched warm-up reported an error")
+    steps = max(1, min(args.steps, 40))
+    ev = []
+    barrier(world)
+    torch.cuda.synchronize()
+    for i in range(steps):
+        prepare(100 + i)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plan.run(stream=stream)
+        b.record(stream)
+        ev.append((a, b))
+    torch.cuda.synchronize()
+    barrier(world)
+    st = plan.status(stream=stream)
+    if st != gbsort.OK:
+        raise RuntimeError(f"batched run reported {gbsort.status_string(st)}")
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = max_over_ranks(world, sum(ms))
+    value = world * steps * n / (total_ms / 1e3) / 1e9
+
+    # device-side check of the last batch: every segment ascending, and each
+    # (key, value) pair is an input pair (values are original indices)
+    prepare(4242)
+    with torch.cuda.stream(stream):
+        orig = keys.clone()
+    plan.run(stream=stream)
+    torch.cuda.synchronize()
+    seg_id = torch.repeat_interleave(torch.arange(len(sizes), device=dev), torch.as_tensor(sizes, device=dev))
+    k64 = keys.to(torch.int64) & 0xFFFFFFFF
+    ordered = bool(((k64[1:] >= k64[:-1]) | (seg_id[1:] != seg_id[:-1])).all().item())
+    paired = bool(torch.equal(orig[vals.to(torch.int64)], keys))
+    in_seg = bool(torch.equal(seg_id[vals.to(torch.int64)], seg_id))
+    ok = ordered and paired and in_seg
+    del k64, orig
+
+    # baseline: the plain sort called once per segment, same GPU and data
+    max_seg = int(sizes.max())
+    tb = gbsort.temp_bytes(kt, max_seg, vb)
+    lws = torch.empty(tb, dtype=torch.uint8, device=dev)
+    loop_ms = []
+    for r in range(2):
+        prepare(300 + r)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        kp, vp = keys.data_ptr(), vals.data_ptr()
+        for s in range(len(sizes)):
+            m = int(sizes[s])
+            o = int(off[s])
+            gbsort.sort(kp + 4 * o, m, kt, lws, tb, values=vp + 4 * o, value_bytes=vb, stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        loop_ms.append(a.elapsed_time(b))
+    loop_value = n / (min(loop_ms) / 1e3) / 1e9
+
+    hbm, peak_kind = peaks()
+    algo_bytes = info["keys_in_cta"] * 2 * (4 + vb) + info["keys_in_onesweep"] * (4 + 4 * 2 * (4 + vb))
+    mean_ms = total_ms / steps
+    if rank != 0:
+        return
+    line = {
+        "metric": "batched segmented sort throughput (Gkeys/s)", "value": round(value, 3), "unit": "Gkeys/s",
+        "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": kt, "data": "synthetic",
+        "config": {"workload": cfg["workload"], "n_keys": n, "segments": len(sizes), "value_bytes": vb,
+                   "paths": {k: info[k] for k in ("cta_small4_segments", "cta_small_segments",
+                                                  "cta_large_segments", "onesweep_segments", "onesweep_tiles",
+                                                  "keys_in_cta", "keys_in_onesweep")},
+                   "graph": "captured on the first run, replayed", "flush": "512 MiB L2 flush before every step"},
+        "loop_baseline": {"value": round(loop_value, 3), "unit": "Gkeys/s", "ms": round(min(loop_ms), 3),
+                          "impl": "gbsort_sort_pairs called once per segment (4096 calls), same GPU and data"},
+        "speedup_vs_loop": round(value / loop_value, 2),
+        "sort_roofline": {"algorithmic_bytes": algo_bytes,
+                          "achieved": round(algo_bytes / (mean_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                          "frac": round(algo_bytes / (mean_ms / 1e3) / 1e9 / hbm, 4),
+                          "note": "CTA-sorted keys move 2*(K+V) bytes, onesweep keys K + P*2*(K+V)"},
+        "autotune": {"seconds": round(tune_s, 1), "report": report.strip().splitlines()},
+        "sorted_check": ok,
+        "gpu_launches": steps * (2 + 4 + 4),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -443,6 +573,8 @@ def main():
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         bench_reference(args, cfg, world, rank)
+    elif "segments" in cfg:
+        bench_batched(args, cfg, world, rank, local)
     else:
         bench_gbsort(args, cfg, world, rank, local)
     if world > 1:

@@ -38,8 +38,9 @@ const KernelEntry* upsweep_entry_for() {
 }
 
 // ---- batched mode ---------------------------------------------------------
-// Small-segment CTA sorts: "S" = 256 threads x 8 items, "L" = 512 threads x
-// as many items as keep the two shared buffers within 128 KB.
+// Small-segment CTA sorts: "S" = 256 threads x 8 items (8- or 4-bit digits),
+// "L" = 512 threads x as many items as keep the two shared buffers within
+// 128 KB (8-bit digits).
 template <int KB, int VB>
 struct CtaShapes {
     static constexpr int S_THREADS = 256, S_IPT = 8;
@@ -48,21 +49,25 @@ struct CtaShapes {
     static constexpr int L_IPT = L_ITEMS_RAW / L_THREADS > 32 ? 32 : (L_ITEMS_RAW / L_THREADS < 4 ? 4 : L_ITEMS_RAW / L_THREADS);
 };
 
+template <int KB, int VB, int THREADS, int IPT, int RBITS>
+KernelEntry make_cta_entry() {
+    using GC = CtaSortGeom<KB, VB, THREADS, IPT, RBITS>;
+    return KernelEntry{reinterpret_cast<const void*>(&cta_sort_kernel<KB, VB, THREADS, IPT, RBITS>), THREADS, IPT,
+                       GC::TILE, static_cast<unsigned long>(GC::SMEM_BYTES)};
+}
+
 template <int KB, int VB>
-void make_seg_entries(KernelEntry* out /* [3]: pass, cta S, cta L */) {
+void make_seg_entries(KernelEntry* out /* [4]: pass, cta S, cta L, cta S 4-bit */) {
     using C = CtaShapes<KB, VB>;
-    using GS = CtaSortGeom<KB, VB, C::S_THREADS, C::S_IPT>;
-    using GL = CtaSortGeom<KB, VB, C::L_THREADS, C::L_IPT>;
     out[0] = make_pass_entry<KB, VB, uint32_t, true>();
-    out[1] = KernelEntry{reinterpret_cast<const void*>(&cta_sort_kernel<KB, VB, C::S_THREADS, C::S_IPT>),
-                         C::S_THREADS, C::S_IPT, GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)};
-    out[2] = KernelEntry{reinterpret_cast<const void*>(&cta_sort_kernel<KB, VB, C::L_THREADS, C::L_IPT>),
-                         C::L_THREADS, C::L_IPT, GL::TILE, static_cast<unsigned long>(GL::SMEM_BYTES)};
+    out[1] = make_cta_entry<KB, VB, C::S_THREADS, C::S_IPT, 8>();
+    out[2] = make_cta_entry<KB, VB, C::L_THREADS, C::L_IPT, 8>();
+    out[3] = make_cta_entry<KB, VB, C::S_THREADS, C::S_IPT, 4>();
 }
 
 template <int KB>
 const KernelEntry* seg_entries_for() {
-    static KernelEntry e[6][3];
+    static KernelEntry e[6][4];
     static const bool init = [] {
         make_seg_entries<KB, 0>(e[0]);
         make_seg_entries<KB, 1>(e[1]);

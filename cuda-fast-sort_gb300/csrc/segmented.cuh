@@ -107,48 +107,75 @@ __global__ void __launch_bounds__(SEG_UP_THREADS) seg_upsweep_kernel(SegUpsweepP
 
 // ---------------------------------------------------------------------------
 // Small segments: whole-segment LSD sort inside one CTA's shared memory.
+// RBITS = bits per digit: 8 (256 bins, shared-memory OR match) or 4 (16
+// bins, twice the passes but tiny scans, 4-ballot match) — the batched
+// sort's tuning picks per size bucket.  Warp-columns holding only filler
+// positions (past the segment's end) are skipped entirely.
 // ---------------------------------------------------------------------------
-template <int KB, int VB, int THREADS, int IPT>
+template <int KB, int VB, int THREADS, int IPT, int RBITS>
 struct CtaSortGeom {
+    static constexpr int BINS = 1 << RBITS;
+    static constexpr int PASSES = KB * 8 / RBITS;
     static constexpr int WARPS = THREADS / 32;
     static constexpr int TILE = THREADS * IPT;  // largest segment
     static constexpr int IPW = 32 * IPT;
     static constexpr size_t KEY_BYTES = size_t(TILE) * KB;
     static constexpr size_t VAL_OFF = (KEY_BYTES + 127) & ~size_t(127);
     static constexpr size_t BUF_BYTES = (VAL_OFF + size_t(TILE) * VB + 127) & ~size_t(127);
-    static constexpr size_t HIST_OFF = 2 * BUF_BYTES;              // u32 [WARPS][256]
-    static constexpr size_t MATCH_OFF = HIST_OFF + size_t(WARPS) * 256 * 4;  // u32 [WARPS][256]
-    static constexpr size_t SCAN_OFF = MATCH_OFF + size_t(WARPS) * 256 * 4;  // u32 [16]
-    static constexpr size_t SEG_OFF = SCAN_OFF + 64;               // SegItem
+    static constexpr size_t HIST_OFF = 2 * BUF_BYTES;                              // u32 [WARPS][BINS]
+    static constexpr size_t MATCH_OFF = HIST_OFF + size_t(WARPS) * BINS * 4;       // u32 [WARPS][256] (RBITS 8)
+    static constexpr size_t SCAN_OFF = MATCH_OFF + (RBITS == 8 ? size_t(WARPS) * 256 * 4 : 0);  // u32 [16]
+    static constexpr size_t SEG_OFF = SCAN_OFF + 64;                               // SegItem
     static constexpr size_t SMEM_BYTES = SEG_OFF + sizeof(SegItem);
-    static_assert(THREADS >= 256, "bin owners need 256 threads");
+    static_assert(RBITS == 8 || RBITS == 4, "8- or 4-bit digits");
+    static_assert(THREADS >= BINS, "one bin owner per digit");
 };
 
-template <int KB, int VB, int THREADS, int IPT>
+template <int RBITS, class U>
+__device__ __forceinline__ uint32_t digit_bits(U x, int pass) {
+    if constexpr (RBITS == 8) return digit_of(x, pass);
+    else return uint32_t(x >> (pass * RBITS)) & ((1u << RBITS) - 1u);
+}
+
+// Lanes holding the same RBITS-bit digit, from one ballot per bit.
+template <int RBITS>
+__device__ __forceinline__ uint32_t match_ballot_bits(uint32_t d) {
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < RBITS; ++bit) {
+        const uint32_t m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+        peers &= ((d >> bit) & 1u) ? m : ~m;
+    }
+    return peers;
+}
+
+template <int KB, int VB, int THREADS, int IPT, int RBITS>
 __global__ void __launch_bounds__(THREADS) cta_sort_kernel(CtaSortParams p) {
     using U = typename KeyBits<KB>::U;
     using V = typename ValBits<VB>::V;
-    using G = CtaSortGeom<KB, VB, THREADS, IPT>;
+    using G = CtaSortGeom<KB, VB, THREADS, IPT, RBITS>;
     constexpr bool PAIRS = VB > 0;
+    constexpr int BINS = G::BINS;
     extern __shared__ __align__(128) uint8_t smem[];
     uint32_t* whist = reinterpret_cast<uint32_t*>(smem + G::HIST_OFF);
     uint32_t* match_scratch = reinterpret_cast<uint32_t*>(smem + G::MATCH_OFF);
     uint32_t* scan32 = reinterpret_cast<uint32_t*>(smem + G::SCAN_OFF);
     SegItem* s_seg = reinterpret_cast<SegItem*>(smem + G::SEG_OFF);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int kind = p.kind, desc = p.desc, passes = p.passes;
-    for (int i = tid; i < G::WARPS * 256; i += THREADS) match_scratch[i] = 0u;
+    const int kind = p.kind, desc = p.desc;
+    if constexpr (RBITS == 8) {
+        for (int i = tid; i < G::WARPS * 256; i += THREADS) match_scratch[i] = 0u;
+    }
     U* gkeys = static_cast<U*>(p.keys);
     V* gvals = static_cast<V*>(p.vals);
     const uint32_t lt = lanemask_lt();
-    uint32_t* wh = whist + warp * 256;
+    uint32_t* wh = whist + warp * BINS;
     uint32_t* mb = match_scratch + warp * 256;
 
     for (;;) {
         if (tid == 0) {
             const uint32_t i = atomicAdd(p.seg_counter, 1u);
             SegItem s{};
-            s.seg = i;
             if (i < p.num_segs) s = p.segs[i];
             s.pad = i < p.num_segs;
             *s_seg = s;
@@ -157,6 +184,7 @@ __global__ void __launch_bounds__(THREADS) cta_sort_kernel(CtaSortParams p) {
         const SegItem sg = *s_seg;
         if (!sg.pad) break;
         const uint32_t cnt = uint32_t(sg.end - sg.begin);
+        auto live = [&](int u) { return uint32_t(warp * G::IPW + u * 32) < cnt; };  // warp-uniform
 
         U keys[IPT];
         V vals[PAIRS ? IPT : 1];
@@ -171,36 +199,50 @@ __global__ void __launch_bounds__(THREADS) cta_sort_kernel(CtaSortParams p) {
             }
         }
         int last_buf = 0;
-        for (int pass = 0; pass < passes; ++pass) {
+        for (int pass = 0; pass < G::PASSES; ++pass) {
             uint8_t* buf = smem + size_t(pass & 1) * G::BUF_BYTES;
             U* sk = reinterpret_cast<U*>(buf);
             V* sv = reinterpret_cast<V*>(buf + G::VAL_OFF);
-#pragma unroll
-            for (int i = lane; i < 256; i += 32) wh[i] = 0u;
+            for (int i = lane; i < BINS; i += 32) wh[i] = 0u;
             __syncwarp();
 #pragma unroll
-            for (int u = 0; u < IPT; ++u) atomicAdd(&wh[digit_of(keys[u], pass)], 1u);
+            for (int u = 0; u < IPT; ++u)
+                if (live(u)) atomicAdd(&wh[digit_bits<RBITS>(keys[u], pass)], 1u);
             __syncthreads();
             uint32_t total = 0;
-            if (tid < 256) {
+            if (tid < BINS) {
 #pragma unroll
                 for (int w = 0; w < G::WARPS; ++w) {
-                    const uint32_t c = whist[w * 256 + tid];
-                    whist[w * 256 + tid] = total;
+                    const uint32_t c = whist[w * BINS + tid];
+                    whist[w * BINS + tid] = total;
                     total += c;
                 }
             }
-            const uint32_t excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
-            if (tid < 256) {
+            uint32_t excl;
+            if constexpr (BINS == 256) {
+                excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
+            } else {  // one warp scans the bins
+                uint32_t v = (tid < BINS) ? total : 0u;
 #pragma unroll
-                for (int w = 0; w < G::WARPS; ++w) whist[w * 256 + tid] += excl;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+                    if (lane >= o) v += y;
+                }
+                excl = v - total;
+            }
+            if (tid < BINS) {
+#pragma unroll
+                for (int w = 0; w < G::WARPS; ++w) whist[w * BINS + tid] += excl;
             }
             __syncthreads();
             uint32_t rank[IPT];
             StaticFor<0, IPT>::run([&](auto uc) {
                 constexpr int u = decltype(uc)::value;
-                const uint32_t d = digit_of(keys[u], pass);
-                const uint32_t peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
+                if (!live(u)) return;
+                const uint32_t d = digit_bits<RBITS>(keys[u], pass);
+                uint32_t peers;
+                if constexpr (RBITS == 8) peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
+                else peers = match_ballot_bits<RBITS>(d);
                 const uint32_t below = __popc(peers & lt);
                 uint32_t old = 0;
                 if (below == 0) old = atomicAdd(&wh[d], uint32_t(__popc(peers)));
@@ -208,14 +250,16 @@ __global__ void __launch_bounds__(THREADS) cta_sort_kernel(CtaSortParams p) {
             });
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
+                if (!live(u)) continue;
                 sk[rank[u]] = keys[u];
                 if constexpr (PAIRS) sv[rank[u]] = vals[u];
             }
             __syncthreads();
             last_buf = pass & 1;
-            if (pass + 1 < passes) {
+            if (pass + 1 < G::PASSES) {
 #pragma unroll
                 for (int u = 0; u < IPT; ++u) {
+                    if (!live(u)) continue;
                     const int j = warp * G::IPW + u * 32 + lane;
                     keys[u] = sk[j];
                     if constexpr (PAIRS) vals[u] = sv[j];

@@ -82,7 +82,7 @@ int path_for(int kb, int vb, uint64_t len, int s_max, int l_max) {
     if (path < 0) path = len <= uint64_t(s_max) ? GBSORT_PATH_CTA_S : len <= uint64_t(l_max) ? GBSORT_PATH_CTA_L
                                                                                           : GBSORT_PATH_ONESWEEP;
     // a path that cannot hold the segment falls through to the next one
-    if (path == GBSORT_PATH_CTA_S && len > uint64_t(s_max)) path = GBSORT_PATH_CTA_L;
+    if ((path == GBSORT_PATH_CTA_S || path == GBSORT_PATH_CTA_S4) && len > uint64_t(s_max)) path = GBSORT_PATH_CTA_L;
     if (path == GBSORT_PATH_CTA_L && len > uint64_t(l_max)) path = GBSORT_PATH_ONESWEEP;
     return path;
 }
@@ -104,16 +104,18 @@ struct SegPlan {
     int key_type = 0, kb = 0, vb = 0, kind = 0, passes = 0, desc = 0;
     uint64_t n_total = 0;
     size_t num_segments = 0;
-    KernelEntry pass{}, cta_s{}, cta_l{}, upsweep{};
-    std::vector<SegItem> small_s, small_l, up_items;
+    KernelEntry pass{}, cta_s{}, cta_l{}, cta_s4{}, upsweep{};
+    std::vector<SegItem> small_s, small_l, small_s4, up_items;
     std::vector<unsigned long long> large_begin;
     std::vector<TileRec> tiles;
     uint64_t keys_in_cta = 0, keys_in_onesweep = 0;
     // workspace layout
     size_t alt_keys_off = 0, alt_vals_off = 0, ctl_off = 0, seg_counts_off = 0, zero_bytes = 0;
     size_t seg_gofs_off = 0, seg_begin_off = 0, tiles_off = 0, up_items_off = 0, small_s_off = 0, small_l_off = 0;
+    size_t small_s4_off = 0;
     size_t status_off = 0, status_bytes = 0, total_bytes = 0;
-    // ctl block: [0..15] tile counters, [16] upsweep items, [17] cta S, [18] cta L, [19] error word
+    // ctl block: [0..15] tile counters, [16] upsweep items, [17] cta S, [18] cta L, [19] error word,
+    // [20] cta S 4-bit
     // bound buffers and the cached graph
     void* keys = nullptr;
     void* vals = nullptr;
@@ -135,10 +137,11 @@ int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t*
     p->passes = int(kb);
     p->desc = descending ? 1 : 0;
     p->num_segments = num;
-    const KernelEntry* se = seg_entries(p->kb) + vi * 3;
+    const KernelEntry* se = seg_entries(p->kb) + vi * 4;
     p->pass = se[0];
     p->cta_s = se[1];
     p->cta_l = se[2];
+    p->cta_s4 = se[3];
     p->upsweep = *seg_upsweep_entry(p->kb);
     int lg = 0;
     while ((1 << (lg + 1)) <= p->passes) ++lg;
@@ -161,6 +164,9 @@ int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t*
         SegItem it{b, e, 0, 0};
         if (path == GBSORT_PATH_CTA_S) {
             p->small_s.push_back(it);
+            p->keys_in_cta += len;
+        } else if (path == GBSORT_PATH_CTA_S4) {
+            p->small_s4.push_back(it);
             p->keys_in_cta += len;
         } else if (path == GBSORT_PATH_CTA_L) {
             p->small_l.push_back(it);
@@ -190,6 +196,7 @@ int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t*
     auto by_size = [](const SegItem& a, const SegItem& b) { return (a.end - a.begin) > (b.end - b.begin); };
     std::stable_sort(p->small_s.begin(), p->small_s.end(), by_size);
     std::stable_sort(p->small_l.begin(), p->small_l.end(), by_size);
+    std::stable_sort(p->small_s4.begin(), p->small_s4.end(), by_size);
     std::stable_sort(p->up_items.begin(), p->up_items.end(), by_size);
 
     const size_t L = p->large_begin.size();
@@ -215,6 +222,8 @@ int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t*
     o = align_up(o + p->small_s.size() * sizeof(SegItem), 256);
     p->small_l_off = o;
     o = align_up(o + p->small_l.size() * sizeof(SegItem), 256);
+    p->small_s4_off = o;
+    o = align_up(o + p->small_s4.size() * sizeof(SegItem), 256);
     p->status_off = o;
     p->status_bytes = p->tiles.size() * 256 * 4;
     o = align_up(o + p->status_bytes, 256);
@@ -292,11 +301,11 @@ int enqueue_segmented(SegPlan* p, cudaStream_t s) {
         cp.seg_counter = ctl + ctr;
         cp.kind = p->kind;
         cp.desc = p->desc;
-        cp.passes = p->passes;
         return launch(k, grid_for(k, v.size()), &cp, s, "segmented CTA sort");
     };
     if ((st = cta_launch(p->cta_l, p->small_l, p->small_l_off, 18))) return st;
     if ((st = cta_launch(p->cta_s, p->small_s, p->small_s_off, 17))) return st;
+    if ((st = cta_launch(p->cta_s4, p->small_s4, p->small_s4_off, 20))) return st;
     if (L) {
         const uint32_t T = uint32_t(p->tiles.size());
         const uint32_t grid = grid_for(p->pass, T);
@@ -338,6 +347,7 @@ int prepare_all(SegPlan* p) {
     }
     if (!p->small_s.empty() && (st = prepare_kernel(p->cta_s))) return st;
     if (!p->small_l.empty() && (st = prepare_kernel(p->cta_l))) return st;
+    if (!p->small_s4.empty() && (st = prepare_kernel(p->cta_s4))) return st;
     return GBSORT_OK;
 }
 
@@ -383,6 +393,7 @@ int gbsort_segmented_plan_info(const gbsort_segmented_plan* p, gbsort_segmented_
     out->num_segments = p->num_segments;
     out->cta_small_segments = p->small_s.size();
     out->cta_large_segments = p->small_l.size();
+    out->cta_small4_segments = p->small_s4.size();
     out->onesweep_segments = p->large_begin.size();
     out->onesweep_tiles = p->tiles.size();
     out->keys_in_cta = p->keys_in_cta;
@@ -415,6 +426,7 @@ int gbsort_segmented_bind(gbsort_segmented_plan* p, void* d_keys, void* d_values
     if (e == cudaSuccess) e = up(p->up_items_off, p->up_items.data(), p->up_items.size() * sizeof(SegItem));
     if (e == cudaSuccess) e = up(p->small_s_off, p->small_s.data(), p->small_s.size() * sizeof(SegItem));
     if (e == cudaSuccess) e = up(p->small_l_off, p->small_l.data(), p->small_l.size() * sizeof(SegItem));
+    if (e == cudaSuccess) e = up(p->small_s4_off, p->small_s4.data(), p->small_s4.size() * sizeof(SegItem));
     if (e == cudaSuccess) e = up(p->seg_begin_off, p->large_begin.data(), p->large_begin.size() * 8);
     if (e != cudaSuccess) {
         set_last_error("segmented table upload", e);
@@ -505,8 +517,9 @@ int gbsort_segmented_sort(int key_type, int descending, void* d_keys, void* d_va
 int gbsort_set_segmented_path(int key_type, size_t value_bytes, int size_log2, int path) {
     const size_t kb = gbsort_key_bytes(key_type);
     const int vi = value_index(int(value_bytes));
-    if (kb == 0 || vi < 0 || size_log2 < -1 || size_log2 >= BUCKETS || path < -1 || path > GBSORT_PATH_ONESWEEP)
+    if (kb == 0 || vi < 0 || size_log2 < -1 || size_log2 >= BUCKETS || path < -1)
         return GBSORT_ERR_INVALID_ARGUMENT;
+    if (path > GBSORT_PATH_CTA_S4) return GBSORT_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     const int wi = width_index(int(kb));
     if (!g_tune_set[wi][vi]) {
@@ -521,12 +534,21 @@ int gbsort_set_segmented_path(int key_type, size_t value_bytes, int size_log2, i
     return GBSORT_OK;
 }
 
+int gbsort_segmented_path_override(int key_type, size_t value_bytes, int size_log2) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    const int vi = value_index(int(value_bytes));
+    if (kb == 0 || vi < 0 || size_log2 < 0 || size_log2 >= BUCKETS) return -1;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const int wi = width_index(int(kb));
+    return g_tune_set[wi][vi] ? g_tune[wi][vi][size_log2] : -1;
+}
+
 int gbsort_get_segmented_path(int key_type, size_t value_bytes, int size_log2) {
     const size_t kb = gbsort_key_bytes(key_type);
     const int vi = value_index(int(value_bytes));
     if (kb == 0 || vi < 0 || size_log2 < 0 || size_log2 >= BUCKETS) return -2;
     const uint64_t len = uint64_t(1) << size_log2;
-    const KernelEntry* se = seg_entries(int(kb)) + vi * 3;
+    const KernelEntry* se = seg_entries(int(kb)) + vi * 4;
     return path_for(int(kb), int(value_bytes), len, se[1].tile, se[2].tile);
 }
 

@@ -96,7 +96,6 @@ struct CtaSortParams {
     uint32_t* seg_counter;      // zeroed
     int kind;
     int desc;
-    int passes;
 };
 
 }  // namespace gbsort

@@ -66,11 +66,11 @@ class SegmentedInfo(ctypes.Structure):
         ("onesweep_tiles", ctypes.c_uint64), ("keys_in_cta", ctypes.c_uint64),
         ("keys_in_onesweep", ctypes.c_uint64), ("cta_small_max", ctypes.c_uint32),
         ("cta_large_max", ctypes.c_uint32), ("onesweep_tile", ctypes.c_uint32), ("pad", ctypes.c_uint32),
-        ("workspace_bytes", ctypes.c_uint64),
+        ("cta_small4_segments", ctypes.c_uint64), ("workspace_bytes", ctypes.c_uint64),
     ]
 
 
-PATH_CTA_S, PATH_CTA_L, PATH_ONESWEEP = 0, 1, 2
+PATH_CTA_S, PATH_CTA_L, PATH_ONESWEEP, PATH_CTA_S4 = 0, 1, 2, 3
 
 _lib = None
 
@@ -335,3 +335,33 @@ def set_segmented_path(key_type, value_bytes: int, size_log2: int, path: int) ->
 
 def get_segmented_path(key_type, value_bytes: int, size_log2: int) -> int:
     return lib().gbsort_get_segmented_path(key_type_id(key_type), value_bytes, size_log2)
+
+
+def autotune_segmented(key_type, value_bytes: int, scratch, scratch_bytes: int, min_log2: int = 4,
+                       max_log2: int = 20, descending: bool = False, stream=None) -> str:
+    """Runs the batched sort's autotuner (installs the winners) and returns
+    its per-bucket report."""
+    f = lib().gbsort_autotune_segmented
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_size_t, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+    buf = ctypes.create_string_buffer(1 << 16)
+    _check(f(key_type_id(key_type), value_bytes, int(descending), min_log2, max_log2, _ptr(scratch), scratch_bytes,
+             _stream(stream), buf, len(buf)), "autotune")
+    return buf.value.decode()
+
+
+def segmented_tuning_text() -> str:
+    f = lib().gbsort_segmented_tuning_text
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    buf = ctypes.create_string_buffer(1 << 16)
+    f(buf, len(buf))
+    return buf.value.decode()
+
+
+def segmented_tuning_load(text: str) -> None:
+    f = lib().gbsort_segmented_tuning_load
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p]
+    _check(f(text.encode()), "tuning load")

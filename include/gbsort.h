@@ -169,7 +169,8 @@ int gbsort_sort_host(int key_type, int descending, void* h_keys,
 enum {
     GBSORT_PATH_CTA_S = 0,    /* whole segment in a 256-thread CTA          */
     GBSORT_PATH_CTA_L = 1,    /* whole segment in a 512-thread CTA          */
-    GBSORT_PATH_ONESWEEP = 2  /* onesweep passes over the global tile list  */
+    GBSORT_PATH_ONESWEEP = 2, /* onesweep passes over the global tile list  */
+    GBSORT_PATH_CTA_S4 = 3    /* as CTA_S with 4-bit digits (16 bins)       */
 };
 
 typedef struct gbsort_segmented_plan gbsort_segmented_plan;
@@ -186,6 +187,7 @@ typedef struct gbsort_segmented_info {
     uint32_t cta_large_max;   /* largest segment the 512-thread CTA sort takes */
     uint32_t onesweep_tile;   /* keys per onesweep tile                        */
     uint32_t pad;
+    uint64_t cta_small4_segments; /* segments on the 4-bit-digit CTA sort      */
     uint64_t workspace_bytes;
 } gbsort_segmented_info;
 
@@ -224,6 +226,24 @@ int gbsort_set_segmented_path(int key_type, size_t value_bytes, int size_log2,
                               int path);
 /* Path a segment of exactly 2^size_log2 keys would take now. */
 int gbsort_get_segmented_path(int key_type, size_t value_bytes, int size_log2);
+/* The table's explicit entry for the bucket (-1: none, built-in thresholds). */
+int gbsort_segmented_path_override(int key_type, size_t value_bytes,
+                                   int size_log2);
+
+/* Autotuner: for each size bucket min_log2..max_log2 times every path that
+ * can hold segments of that size (4-bit and 8-bit CTA sorts of two tile
+ * shapes, onesweep) on synthetic batches built in the caller's device scratch
+ * (no allocation; ~(key + value bytes) * 12 MiB covers every bucket up to
+ * 2^22), and installs the fastest in the tuning table.  A per-bucket report
+ * is written to `report`. */
+int gbsort_autotune_segmented(int key_type, size_t value_bytes, int descending,
+                              int min_log2, int max_log2, void* d_scratch,
+                              size_t scratch_bytes, void* stream, char* report,
+                              size_t report_cap);
+/* Tuning table as text ("key_type value_bytes size_log2 path" per line);
+ * returns the text length.  _load applies such text. */
+int gbsort_segmented_tuning_text(char* buf, size_t cap);
+int gbsort_segmented_tuning_load(const char* text);
 
 /* ------------------------------------------------------------------------ */
 /* Workspace status and bounded waits                                       */

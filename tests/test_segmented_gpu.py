@@ -129,3 +129,27 @@ def test_segments_at_unaligned_offsets(gb, cuda, oracle):
         gb.set_segmented_path("u16", 8, -1, -1)
     ek, ev = _expected(oracle, "u16", raw, vals, off, False)
     assert _eq(k, ek) and _eq(v, ev)
+
+
+def test_autotuner_installs_paths_and_stays_exact(gb, cuda, oracle):
+    scratch_bytes = 160 << 20
+    scratch = cuda.empty(scratch_bytes, dtype=cuda.uint8, device="cuda")
+    try:
+        report = gb.autotune_segmented("u32", 4, scratch, scratch_bytes, 4, 12)
+        lines = [ln for ln in report.splitlines() if ln.startswith("bucket")]
+        assert len(lines) == 9 and all("->" in ln for ln in lines)
+        chosen = {b: gb.get_segmented_path("u32", 4, b) for b in range(4, 13)}
+        assert all(v in (gb.PATH_CTA_S, gb.PATH_CTA_S4, gb.PATH_CTA_L, gb.PATH_ONESWEEP) for v in chosen.values())
+        text = gb.segmented_tuning_text()
+        assert len([ln for ln in text.splitlines() if ln.startswith("2 4 ")]) >= 1
+        rng = np.random.default_rng(21)
+        off = _layout(rng, 200, 4, 13)
+        n = int(off[-1])
+        raw = raw_keys("u32", n, seed=8)
+        vals = np.arange(n, dtype=np.uint32)
+        (r, v0, k, v), = _run(gb, cuda, "u32", raw, vals, off, False)[0]
+        ek, ev = _expected(oracle, "u32", raw, vals, off, False)
+        assert _eq(k, ek) and _eq(v, ev)
+        gb.segmented_tuning_load(text)  # round trip
+    finally:
+        gb.set_segmented_path("u32", 4, -1, -1)
