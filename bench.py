@@ -61,6 +61,11 @@ CONFIGS = {
     "c4": dict(key="u32", n=0, dist=0, vb=4, desc=False, segments=4096, seg_log2=(8, 20),
                workload="batched: 4096 independent u32-key/u32-value sorts, segment lengths log-uniform in "
                         "[2^8, 2^20] (seeded), keys uniform 32-bit, ascending, one batched run per step"),
+    "c5": dict(key="mixed", n=0, dist=0, vb=4, desc=False, serving=True, size_log2=(10, 24), pool=64 << 30,
+               streams=3, load=0.7,
+               workload="serving: Poisson arrivals, request sizes log-uniform in [2^10, 2^24], key type u32 / u64 / "
+                        "f32 with equal probability, 50% carry u32 values, ascending, host pinned buffers, "
+                        "64 GiB device pool"),
 }
 KEY_BYTES = {"u32": 4, "f32": 4, "u64": 8, "u128": 16}
 FALLBACK_HBM_GBS = 6800.0
@@ -551,7 +556,243 @@ def bench_batched(args, cfg, world, rank, local):
                           "note": "CTA-sorted keys move 2*(K+V) bytes, onesweep keys K + P*2*(K+V)"},
         "autotune": {"seconds": round(tune_s, 1), "report": report.strip().splitlines()},
         "sorted_check": ok,
-        "gpu_launches": steps * (2 + 4 + 4),
+        "gpu_launches": steps * (info["kernel_launches"] + 2),
+        "gpu_launches_note": "per step: the batched run's kernels plus two input-generation kernels",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_serving(args, cfg, world, rank, local):
+    """Sort server (continuous batching) fed from pinned host buffers.
+
+    Phase 1, capacity: a backlog of requests is submitted at once and the
+    time to drain it gives the sustained throughput (value).  Phase 2, load:
+    Poisson arrivals at `--rate` (default: cfg load x capacity) give the
+    p50/p99 latency from submit to result-in-host-memory.  A sample of
+    requests gets its own output buffers and is compared, bit for bit, with
+    the same request sorted alone by the plain sort."""
+    import numpy as np
+    import torch
+
+    import gbsort
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(5150 + rank)
+    lo, hi = cfg["size_log2"]
+    pool_keys = 1 << (hi + 1)
+    types = ("u32", "u64", "f32")
+    dist = {"u32": 0, "u64": 0, "f32": 1}
+    host_in = {}
+    for i, kt in enumerate(types):
+        d = torch.empty(pool_keys * KEY_BYTES[kt], dtype=torch.uint8, device=dev)
+        gbsort.generate(dist[kt], KEY_BYTES[kt], d, pool_keys, 71 + i)
+        torch.cuda.synchronize()
+        host_in[kt] = d.cpu().pin_memory()
+        del d
+    vals_in = torch.arange(pool_keys, dtype=torch.int32).pin_memory()
+    # outputs of unchecked requests land in one shared pinned scratch area
+    out_keys = torch.empty((1 << hi) * 8, dtype=torch.uint8).pin_memory()
+    out_vals = torch.empty((1 << hi) * 4, dtype=torch.uint8).pin_memory()
+
+    def draw():
+        kt = types[int(rng.integers(3))]
+        n = int(np.floor(2.0 ** rng.uniform(lo, hi)))
+        has_v = bool(rng.random() < 0.5)
+        off = int(rng.integers(0, pool_keys - n + 1))
+        return kt, n, has_v, off
+
+    checks = []
+    check_out = {}
+
+    def plan_checks(reqs, tag):
+        """Pinned outputs of every 64th request, allocated before timing."""
+        for i, (kt, n, has_v, off) in enumerate(reqs):
+            if i % 64 == 0:
+                ko = torch.empty(n * KEY_BYTES[kt], dtype=torch.uint8).pin_memory()
+                vo = torch.empty(n * 4, dtype=torch.uint8).pin_memory() if has_v else None
+                check_out[(tag, i)] = (ko, vo)
+                checks.append((reqs[i], ko, vo))
+
+    def submit(srv, req, key=None):
+        kt, n, has_v, off = req
+        kb = KEY_BYTES[kt]
+        kin = host_in[kt].data_ptr() + off * kb
+        vin = vals_in.data_ptr() + off * 4 if has_v else None
+        if key in check_out:
+            ko, vo = check_out[key]
+            kout, vout = ko.data_ptr(), (vo.data_ptr() if has_v else None)
+        else:
+            kout, vout = out_keys.data_ptr(), (out_vals.data_ptr() if has_v else None)
+        return srv.submit(kt, n, kin, kout, vin, vout, value_bytes=4 if has_v else 0)
+
+    # host link: plain pinned copies of 256 MiB each way
+    probe = host_in["u64"]
+    dprobe = torch.empty(probe.numel(), dtype=torch.uint8, device=dev)
+    link = {}
+    for name, dst, src in (("h2d_gbs", dprobe, probe), ("d2h_gbs", probe, dprobe)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(4):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        link[name] = round(4 * probe.numel() / (time.perf_counter() - t1) / 1e9, 1)
+    # both directions at once (the serving pattern): H2D of one buffer while
+    # another comes back, on two streams
+    probe2 = host_in["u32"]
+    dprobe2 = torch.empty(probe2.numel(), dtype=torch.uint8, device=dev)
+    s_up, s_dn = torch.cuda.Stream(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(4):
+        with torch.cuda.stream(s_up):
+            dprobe.copy_(probe, non_blocking=True)
+        with torch.cuda.stream(s_dn):
+            out_keys[:probe2.numel()].copy_(dprobe2, non_blocking=True)
+    torch.cuda.synchronize()
+    link["bidir_gbs"] = round(4 * (probe.numel() + probe2.numel()) / (time.perf_counter() - t1) / 1e9, 1)
+    del dprobe, dprobe2
+
+    srv = gbsort.Server(pool_bytes=cfg["pool"], streams=cfg["streams"])
+    # warm-up: every kernel shape once
+    for _ in range(max(3, args.warmup) * 10):
+        submit(srv, draw())
+    if srv.drain(600.0) != gbsort.OK:
+        raise RuntimeError("server warm-up did not drain")
+
+    # phase 1: capacity under a backlog
+    n_cap = max(200, args.steps * 20)
+    reqs = [draw() for _ in range(n_cap)]
+    plan_checks(reqs, "cap")
+    keys_cap = sum(r[1] for r in reqs)
+    bytes_in = sum(r[1] * (KEY_BYTES[r[0]] + (4 if r[2] else 0)) for r in reqs)
+    srv.reset_stats()
+    clock = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tickets = [submit(srv, r, ("cap", i)) for i, r in enumerate(reqs)]
+    if srv.drain(1200.0) != gbsort.OK:
+        raise RuntimeError("server did not drain")
+    t_cap = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = clock.stop()
+    cap_stats = srv.stats()
+    bad = [t for t in tickets if srv.poll(t) != gbsort.OK]
+    t_cap = max_over_ranks(world, t_cap)
+    value = world * keys_cap / t_cap / 1e9
+    cap_rps = n_cap / t_cap
+
+    # phase 2: Poisson arrivals at a fraction of capacity
+    rate = args.rate if args.rate > 0 else cfg["load"] * cap_rps
+    n_load = max(200, args.steps * 10)
+    reqs2 = [draw() for _ in range(n_load)]
+    plan_checks(reqs2, "load")
+    gaps = rng.exponential(1.0 / rate, n_load)
+    srv.reset_stats()
+    late = 0.0
+    t0 = time.perf_counter()
+    t_next = t0
+    tickets2 = []
+    for i, r in enumerate(reqs2):
+        t_next += gaps[i]
+        while True:
+            now = time.perf_counter()
+            if now >= t_next:
+                break
+            if t_next - now > 2e-4:
+                time.sleep((t_next - now) * 0.5)
+        late = max(late, now - t_next)
+        tickets2.append(submit(srv, r, ("load", i)))
+    if srv.drain(1200.0) != gbsort.OK:
+        raise RuntimeError("server did not drain under load")
+    t_load = time.perf_counter() - t0
+    load_stats = srv.stats()
+    bad += [t for t in tickets2 if srv.poll(t) != gbsort.OK]
+    srv.close()
+
+    # alone vs in the mix: the checked requests, re-sorted by the plain sort
+    same = 0
+    for (kt, n, has_v, off), ko, vo in checks:
+        kb = KEY_BYTES[kt]
+        dk = host_in[kt][off * kb:(off + n) * kb].to(dev)
+        dv = vals_in[off:off + n].to(dev) if has_v else None
+        tb = gbsort.temp_bytes(kt, n, 4 if has_v else 0)
+        ws = torch.empty(tb, dtype=torch.uint8, device=dev)
+        gbsort.sort(dk, n, kt, ws, tb, values=dv, value_bytes=4 if has_v else 0)
+        torch.cuda.synchronize()
+        ok = torch.equal(dk.cpu(), ko) and (not has_v or torch.equal(dv.cpu().view(torch.uint8), vo))
+        same += int(ok)
+    identical = same == len(checks) and not bad
+
+    # CPU oracle on a bounded sample of requests (1 thread)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        import _oracle
+
+        oracle = _oracle.load()
+        budget = min(args.cpu_seconds, 20.0)
+        done_keys, spent, count = 0, 0.0, 0
+        while spent < budget and count < 200:
+            kt, n, has_v, off = draw()
+            kb = KEY_BYTES[kt]
+            raw = host_in[kt][off * kb:(off + n) * kb].numpy().view(np.uint32 if kb == 4 else np.uint64).copy()
+            v = vals_in[off:off + n].numpy().view(np.uint32).copy() if has_v else None
+            t1 = time.perf_counter()
+            oracle.sort(kt, raw, False, v)
+            spent += time.perf_counter() - t1
+            done_keys += n
+            count += 1
+        cpu = {"value": round(done_keys / spent / 1e9, 5), "unit": "Gkeys/s", "cores": 1, "kind": "port",
+               "sample": f"{count} requests of the same distribution ({done_keys} keys), std::stable_sort of "
+                         f"twiddled keys, 1 thread, sorting only (no copies)"}
+    if rank != 0:
+        return
+    mean_keys = keys_cap / n_cap
+    hbm, _ = peaks()
+    line = {
+        "metric": "serving throughput (Gkeys/s) under continuous batching, p50/p99 latency at load",
+        "value": round(value, 3), "unit": "Gkeys/s", "n_gpus": world, "steps": n_cap, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t_cap / n_cap, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32/u64/f32 keys, u32 values", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "step": "one request (capacity phase: backlog of all requests)",
+                   "requests_capacity_phase": n_cap, "requests_load_phase": n_load,
+                   "mean_request_keys": round(mean_keys), "pool_bytes": cfg["pool"], "streams": cfg["streams"],
+                   "flush": "inputs (1.5 GiB of pinned host pools) larger than L2; every request is copied in"},
+        "capacity": {"seconds": round(t_cap, 4), "requests_per_s": round(cap_rps, 1),
+                     "batches": cap_stats["batches"], "mean_batch_requests": round(cap_stats["mean_batch_requests"], 2),
+                     "max_batch_requests": cap_stats["max_batch_requests"],
+                     "pool_peak_gib": round(cap_stats["pool_peak_bytes"] / 2**30, 2),
+                     "link_gbs": round(2 * bytes_in / t_cap / 1e9, 1), "link_probe": link,
+                     "host_plan_s": round(cap_stats["host_plan_seconds"], 4),
+                     "host_launch_s": round(cap_stats["host_launch_seconds"], 4),
+                     "batch_s_sum": round(cap_stats["batch_seconds"], 4),
+                     "stage_device_s": {"h2d": round(cap_stats["h2d_seconds"], 4),
+                                        "sort": round(cap_stats["sort_seconds"], 4),
+                                        "d2h": round(cap_stats["d2h_seconds"], 4)}},
+        "latency": {"rate_rps": round(rate, 1), "load_fraction": round(rate / cap_rps, 3),
+                    "p50_ms": round(load_stats["latency_p50_us"] / 1e3, 3),
+                    "p99_ms": round(load_stats["latency_p99_us"] / 1e3, 3),
+                    "mean_ms": round(load_stats["latency_mean_us"] / 1e3, 3),
+                    "max_ms": round(load_stats["latency_max_us"] / 1e3, 3),
+                    "queue_p50_ms": round(load_stats["queue_p50_us"] / 1e3, 3),
+                    "queue_p99_ms": round(load_stats["queue_p99_us"] / 1e3, 3),
+                    "sustained_gkeys": round(load_stats["keys_sorted"] / max(load_stats["active_seconds"], 1e-9)
+                                             / 1e9, 3),
+                    "mean_batch_requests": round(load_stats["mean_batch_requests"], 2),
+                    "arrival_max_late_ms": round(1e3 * late, 3), "seconds": round(t_load, 3)},
+        "e2e": {"value": round(value, 3), "unit": "Gkeys/s", "h2d_bytes_per_step": int(bytes_in / n_cap),
+                "d2h_bytes_per_step": int(bytes_in / n_cap),
+                "api": "gbsort_server_submit / drain with pinned HOST buffers (value is already end to end)"},
+        "roofline": {"bound": "hbm", "note": "the server's kernels are the batched sort's; host link bytes in "
+                                             "capacity.link_gbs", "peak": hbm, "unit": "GB/s"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": cap_stats["kernel_launches"],
+        "identical_alone_and_in_mix": identical, "checked_requests": len(checks), "failed_requests": len(bad),
     }
     print(json.dumps(line), flush=True)
 
@@ -567,12 +808,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cub", action="store_true", help="skip the CUB comparator")
+    ap.add_argument("--rate", type=float, default=0.0,
+                    help="c5: Poisson arrival rate in requests/s (0: the configured fraction of measured capacity)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # timing rule: at least 3 warm-up steps
     world, rank, local = dist_init()
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         bench_reference(args, cfg, world, rank)
+    elif cfg.get("serving"):
+        bench_serving(args, cfg, world, rank, local)
     elif "segments" in cfg:
         bench_batched(args, cfg, world, rank, local)
     else:

@@ -34,6 +34,17 @@ enum : uint32_t { ERRBIT_TIMEOUT = 1u, ERRBIT_BOUNDS = 2u };
 // Lookback: issue the window's reads before the rank (1) or after it (0).
 // Measured equal on GB300 (2^28 u32: 66.9 vs 67.2 Gkeys/s); 0 keeps the
 // registers free during the rank.
+// Tiles a pass CTA claims beyond the one it is ranking.  1 (default): the
+// next tile is claimed when the current one starts, so tiles are ranked in
+// about the order they were claimed.  3: the two ids after next are claimed
+// early too, hiding the atomic's and the table load's latency, but a CTA
+// then sits on claims its successors wait for; when CTAs start staggered
+// (another kernel releasing the SMs one by one) the lookback degenerates into
+// a serial chain, ~35x slower on GB300, and even alone it is not faster.
+#ifndef GBSORT_TILE_LOOKAHEAD
+#define GBSORT_TILE_LOOKAHEAD 1
+#endif
+
 #ifndef GBSORT_LOOKBACK_PREFETCH
 #define GBSORT_LOOKBACK_PREFETCH 0
 #endif

@@ -268,10 +268,9 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
             bulk_copy_g2s(buf + G::VAL_OFF, reinterpret_cast<const void*>(va - mv), vbytes, &mbar[slot], pol);
     };
 
-    // Tile ids come from the pass's atomic counter three tiles ahead: thread 0
-    // holds the next tile (being copied), the one after (its table entry
-    // loading) and the one after that (its id in flight), so neither the
-    // atomic's nor the table load's latency stalls a tile.
+    // Tile ids come from the pass's atomic counter.  Thread 0 claims the next
+    // tile when the current one starts and bulk-copies it into the other
+    // buffer meanwhile (GBSORT_TILE_LOOKAHEAD 3 claims two more ahead).
     uint32_t id_an = 0, id_aan = 0;  // thread 0: ids of the tiles after next
     TileRec rec_an{};                // thread 0: table entry of id_an
     __syncthreads();
@@ -280,9 +279,11 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         const TileInfo i0 = make_info(t0, load_rec(t0));
         info_slot[0] = i0;
         if (t0 < T) issue_tile(i0, 0);
+#if GBSORT_TILE_LOOKAHEAD >= 3
         id_an = t0 < T ? atomicAdd(p.tile_counter, 1u) : T;
         rec_an = load_rec(id_an);
         id_aan = id_an < T ? atomicAdd(p.tile_counter, 1u) : T;
+#endif
     }
     __syncthreads();
     TileInfo cur = info_slot[0];
@@ -293,15 +294,22 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     while (cur.id < T) {
         const int b = int(it & 1u);
         if (tid == 0) {
+#if GBSORT_TILE_LOOKAHEAD >= 3
             const TileInfo ni = make_info(id_an, rec_an);
+#else  // claim the next tile only now: a CTA holds two claims at most
+            const uint32_t nid = atomicAdd(p.tile_counter, 1u);
+            const TileInfo ni = make_info(nid, load_rec(nid));
+#endif
             info_slot[(it + 1) & 1u] = ni;
             next_issued = ni.id < T;
             if (next_issued) {
                 fence_proxy_async_smem();
                 issue_tile(ni, b ^ 1);
+#if GBSORT_TILE_LOOKAHEAD >= 3
                 rec_an = load_rec(id_aan);
                 id_an = id_aan;
                 id_aan = id_aan < T ? atomicAdd(p.tile_counter, 1u) : T;
+#endif
             }
         }
         unsigned long long seg_base_d = 0;  // batched: this tile's segment's digit base (bin owners)

@@ -108,6 +108,7 @@ struct SegPlan {
     std::vector<SegItem> small_s, small_l, small_s4, up_items;
     std::vector<unsigned long long> large_begin;
     std::vector<TileRec> tiles;
+    std::vector<uint8_t> image;  // host copy of the tables for the pageable upload
     uint64_t keys_in_cta = 0, keys_in_onesweep = 0;
     // workspace layout
     size_t alt_keys_off = 0, alt_vals_off = 0, ctl_off = 0, seg_counts_off = 0, zero_bytes = 0;
@@ -402,11 +403,36 @@ int gbsort_segmented_plan_info(const gbsort_segmented_plan* p, gbsort_segmented_
     out->cta_large_max = uint32_t(p->cta_l.tile);
     out->onesweep_tile = uint32_t(p->pass.tile);
     out->workspace_bytes = p->total_bytes;
+    out->kernel_launches = (p->large_begin.empty() ? 0 : 2 + uint64_t(p->passes)) + !p->small_l.empty() +
+                           !p->small_s.empty() + !p->small_s4.empty();
     return GBSORT_OK;
 }
 
-int gbsort_segmented_bind(gbsort_segmented_plan* p, void* d_keys, void* d_values, void* d_workspace,
-                          size_t workspace_bytes, void* stream) {
+}  // extern "C"
+
+namespace gbsort {
+
+size_t segmented_table_bytes(const gbsort_segmented_plan* p) { return p->status_off - p->seg_begin_off; }
+
+// Host image of the workspace range [seg_begin_off, status_off): segment
+// begins, tile list, upsweep items, CTA segment lists.
+void segmented_table_image(const gbsort_segmented_plan* p, uint8_t* dst) {
+    std::memset(dst, 0, segmented_table_bytes(p));
+    auto put = [&](size_t off, const void* src, size_t bytes) {
+        if (bytes) std::memcpy(dst + (off - p->seg_begin_off), src, bytes);
+    };
+    put(p->seg_begin_off, p->large_begin.data(), p->large_begin.size() * 8);
+    put(p->tiles_off, p->tiles.data(), p->tiles.size() * sizeof(TileRec));
+    put(p->up_items_off, p->up_items.data(), p->up_items.size() * sizeof(SegItem));
+    put(p->small_s_off, p->small_s.data(), p->small_s.size() * sizeof(SegItem));
+    put(p->small_l_off, p->small_l.data(), p->small_l.size() * sizeof(SegItem));
+    put(p->small_s4_off, p->small_s4.data(), p->small_s4.size() * sizeof(SegItem));
+}
+
+// bind with the table image taken from `image` (pinned memory lets the
+// upload run asynchronously); image == nullptr builds it in pageable memory.
+int segmented_bind_image(gbsort_segmented_plan* p, void* d_keys, void* d_values, void* d_workspace,
+                         size_t workspace_bytes, void* stream, const uint8_t* image) {
     if (!p || (p->num_segments && !d_keys) || (p->vb && p->num_segments && !d_values)) return GBSORT_ERR_INVALID_ARGUMENT;
     if (d_workspace == nullptr || workspace_bytes < p->total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
     if ((reinterpret_cast<uintptr_t>(d_keys) % p->kb) || (p->vb && reinterpret_cast<uintptr_t>(d_values) % p->vb))
@@ -418,21 +444,31 @@ int gbsort_segmented_bind(gbsort_segmented_plan* p, void* d_keys, void* d_values
     p->keys = d_keys;
     p->vals = d_values;
     p->ws = static_cast<uint8_t*>(d_workspace);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    auto up = [&](size_t off, const void* src, size_t bytes) {
-        return bytes ? cudaMemcpyAsync(p->ws + off, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
-    };
-    cudaError_t e = up(p->tiles_off, p->tiles.data(), p->tiles.size() * sizeof(TileRec));
-    if (e == cudaSuccess) e = up(p->up_items_off, p->up_items.data(), p->up_items.size() * sizeof(SegItem));
-    if (e == cudaSuccess) e = up(p->small_s_off, p->small_s.data(), p->small_s.size() * sizeof(SegItem));
-    if (e == cudaSuccess) e = up(p->small_l_off, p->small_l.data(), p->small_l.size() * sizeof(SegItem));
-    if (e == cudaSuccess) e = up(p->small_s4_off, p->small_s4.data(), p->small_s4.size() * sizeof(SegItem));
-    if (e == cudaSuccess) e = up(p->seg_begin_off, p->large_begin.data(), p->large_begin.size() * 8);
+    // the tables sit back to back in the workspace: upload them as one image
+    const size_t bytes = segmented_table_bytes(p);
+    if (bytes == 0) return GBSORT_OK;
+    const uint8_t* src = image;
+    if (src == nullptr) {  // kept with the plan: the copy may read it later
+        p->image.resize(bytes);
+        segmented_table_image(p, p->image.data());
+        src = p->image.data();
+    }
+    const cudaError_t e = cudaMemcpyAsync(p->ws + p->seg_begin_off, src, bytes, cudaMemcpyHostToDevice,
+                                          static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) {
         set_last_error("segmented table upload", e);
         return GBSORT_ERR_CUDA;
     }
     return GBSORT_OK;
+}
+
+}  // namespace gbsort
+
+extern "C" {
+
+int gbsort_segmented_bind(gbsort_segmented_plan* p, void* d_keys, void* d_values, void* d_workspace,
+                          size_t workspace_bytes, void* stream) {
+    return gbsort::segmented_bind_image(p, d_keys, d_values, d_workspace, workspace_bytes, stream, nullptr);
 }
 
 // Runs the bound plan.  use_graph != 0: the first run captures the launch
@@ -553,3 +589,11 @@ int gbsort_get_segmented_path(int key_type, size_t value_bytes, int size_log2) {
 }
 
 }  // extern "C"
+
+namespace gbsort {
+// Device address of a bound plan's error word (the sort server copies it to
+// pinned host memory at the end of each batch instead of synchronizing).
+const void* segmented_error_word(const gbsort_segmented_plan* p) {
+    return (p && p->ws) ? p->ws + p->ctl_off + 19 * 4 : nullptr;
+}
+}  // namespace gbsort

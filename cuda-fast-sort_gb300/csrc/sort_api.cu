@@ -14,6 +14,7 @@
 
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -167,9 +168,16 @@ int prepare_kernel(const KernelEntry& e) {
     return p ? p->status : GBSORT_ERR_CUDA;
 }
 
+// Persistent CTAs per SM of a kernel: its occupancy, capped by the
+// GBSORT_CTAS_PER_SM environment variable when set (a tuning knob).
 int resident_ctas(const KernelEntry& e) {
+    static const int cap = [] {
+        const char* v = std::getenv("GBSORT_CTAS_PER_SM");
+        return v ? std::atoi(v) : 0;
+    }();
     KernelPrep* p = prep_for(e);
-    return p ? p->occ : 0;
+    const int occ = p ? p->occ : 0;
+    return (cap > 0 && occ > cap) ? cap : occ;
 }
 
 int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
@@ -499,6 +507,21 @@ int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n, void* d_
         return GBSORT_ERR_CUDA;
     }
     return status_from_error_word(err);
+}
+
+int gbsort_workspace_reset(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {
+    Plan plan;
+    int st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (d_workspace == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (n == 0) return GBSORT_OK;
+    const cudaError_t e = cudaMemsetAsync(static_cast<uint8_t*>(d_workspace) + plan.ctl_off, 0, plan.ctl.bytes,
+                                          static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        set_last_error("workspace reset", e);
+        return GBSORT_ERR_CUDA;
+    }
+    return GBSORT_OK;
 }
 
 void gbsort_set_wait_limit_ns(uint64_t ns) { g_wait_limit_ns.store(ns, std::memory_order_relaxed); }

@@ -67,6 +67,7 @@ class SegmentedInfo(ctypes.Structure):
         ("keys_in_onesweep", ctypes.c_uint64), ("cta_small_max", ctypes.c_uint32),
         ("cta_large_max", ctypes.c_uint32), ("onesweep_tile", ctypes.c_uint32), ("pad", ctypes.c_uint32),
         ("cta_small4_segments", ctypes.c_uint64), ("workspace_bytes", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
     ]
 
 
@@ -365,3 +366,128 @@ def segmented_tuning_load(text: str) -> None:
     f.restype = ctypes.c_int
     f.argtypes = [ctypes.c_char_p]
     _check(f(text.encode()), "tuning load")
+
+
+# ---- sort server (continuous batching) --------------------------------------
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("pool_bytes", ctypes.c_uint64), ("streams", ctypes.c_uint32), ("paused", ctypes.c_uint32),
+                ("max_batch_keys", ctypes.c_uint64), ("max_batch_requests", ctypes.c_uint64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("key_type", ctypes.c_int), ("descending", ctypes.c_int), ("value_bytes", ctypes.c_size_t),
+                ("n", ctypes.c_size_t), ("keys_in", ctypes.c_void_p), ("values_in", ctypes.c_void_p),
+                ("keys_out", ctypes.c_void_p), ("values_out", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("submitted", "completed", "failed", "rejected", "batches",
+                                               "max_batch_requests", "keys_sorted", "bytes_sorted", "pool_bytes",
+                                               "pool_peak_bytes", "kernel_launches")] + \
+               [(f, ctypes.c_double) for f in ("latency_p50_us", "latency_p99_us", "latency_mean_us",
+                                               "latency_max_us", "queue_p50_us", "queue_p99_us",
+                                               "mean_batch_requests", "active_seconds", "host_plan_seconds",
+                                               "host_launch_seconds", "batch_seconds", "h2d_seconds",
+                                               "sort_seconds", "d2h_seconds")]
+
+
+def _declare_server(l) -> None:
+    vp, i, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64
+    sig = {
+        "gbsort_server_create": (i, [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+        "gbsort_server_destroy": (None, [vp]),
+        "gbsort_server_submit": (i, [vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+        "gbsort_server_poll": (i, [vp, u64]),
+        "gbsort_server_wait": (i, [vp, u64, u64]),
+        "gbsort_server_drain": (i, [vp, u64]),
+        "gbsort_server_pause": (i, [vp]),
+        "gbsort_server_resume": (i, [vp]),
+        "gbsort_server_stats_get": (i, [vp, ctypes.POINTER(ServerStats)]),
+        "gbsort_server_stats_reset": (i, [vp]),
+        "gbsort_workspace_reset": (i, [i, ctypes.c_size_t, ctypes.c_size_t, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(l, name)
+        f.restype = res
+        f.argtypes = args
+
+
+class Server:
+    """Continuous-batching sort server (gbsort_server_*): submit requests
+    from host or device buffers, poll/wait per ticket; queued requests of one
+    class are coalesced into batched sorts, admitted by bytes against a
+    pooled device allocation, with several batches in flight."""
+
+    def __init__(self, pool_bytes: int = 0, streams: int = 0, paused: bool = False, max_batch_keys: int = 0,
+                 max_batch_requests: int = 0):
+        _declare_server(lib())
+        cfg = ServerConfig(pool_bytes, streams, int(paused), max_batch_keys, max_batch_requests)
+        h = ctypes.c_void_p()
+        _check(lib().gbsort_server_create(ctypes.byref(cfg), ctypes.byref(h)), "server create")
+        self.handle = h
+
+    def submit(self, key_type, n: int, keys_in, keys_out=None, values_in=None, values_out=None,
+               value_bytes: int = 0, descending: bool = False) -> int:
+        """Pointers are ints or tensors (host or device); keys_out defaults
+        to keys_in (in place).  Returns the ticket."""
+        keys_out = keys_in if keys_out is None else keys_out
+        values_out = values_in if values_out is None else values_out
+        r = Request(key_type_id(key_type), int(descending), value_bytes, n, _ptr(keys_in), _ptr(values_in),
+                    _ptr(keys_out), _ptr(values_out))
+        t = ctypes.c_uint64()
+        _check(lib().gbsort_server_submit(self.handle, ctypes.byref(r), ctypes.byref(t)), "server submit")
+        return t.value
+
+    def try_submit(self, *args, **kw):
+        """As submit, but returns (status, ticket) instead of raising."""
+        try:
+            return OK, self.submit(*args, **kw)
+        except GbsortError as e:
+            return e.status, None
+
+    def poll(self, ticket: int) -> int:
+        return lib().gbsort_server_poll(self.handle, ticket)
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> int:
+        return lib().gbsort_server_wait(self.handle, ticket, int(timeout_s * 1e9))
+
+    def drain(self, timeout_s: float = 600.0) -> int:
+        return lib().gbsort_server_drain(self.handle, int(timeout_s * 1e9))
+
+    def pause(self) -> None:
+        _check(lib().gbsort_server_pause(self.handle), "server pause")
+
+    def resume(self) -> None:
+        _check(lib().gbsort_server_resume(self.handle), "server resume")
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(lib().gbsort_server_stats_get(self.handle, ctypes.byref(s)), "server stats")
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        _check(lib().gbsort_server_stats_reset(self.handle), "server stats reset")
+
+    def close(self) -> None:
+        if self.handle:
+            lib().gbsort_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def workspace_reset(key_type, n: int, workspace, value_bytes: int = 0, stream=None) -> None:
+    _declare_server(lib())
+    _check(lib().gbsort_workspace_reset(key_type_id(key_type), value_bytes, n, _ptr(workspace), _stream(stream)),
+           "workspace reset")

@@ -189,6 +189,7 @@ typedef struct gbsort_segmented_info {
     uint32_t pad;
     uint64_t cta_small4_segments; /* segments on the 4-bit-digit CTA sort      */
     uint64_t workspace_bytes;
+    uint64_t kernel_launches; /* kernels one run launches (plus one memset)  */
 } gbsort_segmented_info;
 
 /* Plan from HOST offsets (num_segments + 1 entries, non-decreasing). */
@@ -246,8 +247,92 @@ int gbsort_segmented_tuning_text(char* buf, size_t cap);
 int gbsort_segmented_tuning_load(const char* text);
 
 /* ------------------------------------------------------------------------ */
+/* Sort server — continuous batching of independent sort requests.  No      */
+/* counterpart in the reference.  Requests arrive from any thread; one      */
+/* scheduler thread coalesces queued requests of one class (key type, value */
+/* size, order) into a batched sort over a contiguous staging area carved   */
+/* from one pooled device allocation, admits a batch only when its bytes    */
+/* fit the pool, and keeps up to `streams` batches in flight, so the copies */
+/* of one batch overlap the sort of another.  A request's buffers may be    */
+/* host (pinned for overlap) or device memory; results land in keys_out /   */
+/* values_out (which may equal the inputs).                                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbsort_server gbsort_server;
+
+typedef struct gbsort_server_config {
+    uint64_t pool_bytes;      /* device pool = admission budget (0: 64 GiB)  */
+    uint32_t streams;         /* batches in flight (0: 3)                    */
+    uint32_t paused;          /* start paused (see gbsort_server_resume)     */
+    uint64_t max_batch_keys;  /* keys coalesced into one launch (0: 2^26)    */
+    uint64_t max_batch_requests; /* requests per launch (0: 4096)            */
+} gbsort_server_config;
+
+typedef struct gbsort_request {
+    int key_type;
+    int descending;
+    size_t value_bytes;       /* 0: keys only                                */
+    size_t n;
+    const void* keys_in;      /* host or device memory                       */
+    const void* values_in;
+    void* keys_out;           /* may equal keys_in                           */
+    void* values_out;
+} gbsort_request;
+
+typedef struct gbsort_server_stats {
+    uint64_t submitted, completed, failed, rejected;
+    uint64_t batches;
+    uint64_t max_batch_requests;
+    uint64_t keys_sorted;     /* keys of completed requests                  */
+    uint64_t bytes_sorted;    /* key + value bytes of completed requests     */
+    uint64_t pool_bytes;
+    uint64_t pool_peak_bytes; /* high-water mark of the pool in use          */
+    uint64_t kernel_launches; /* kernels launched by the batches             */
+    double latency_p50_us, latency_p99_us, latency_mean_us, latency_max_us;
+    double queue_p50_us, queue_p99_us; /* submit -> batch launch             */
+    double mean_batch_requests;
+    double active_seconds;    /* first submit -> last completion             */
+    double host_plan_seconds; /* scheduler time forming and sizing batches   */
+    double host_launch_seconds; /* scheduler time enqueuing batches          */
+    double batch_seconds;     /* sum over batches of launch -> completion    */
+    double h2d_seconds;       /* device time of the batches' input copies    */
+    double sort_seconds;      /* device time of the batches' sorts           */
+    double d2h_seconds;       /* device time of the batches' output copies   */
+} gbsort_server_stats;
+
+/* cfg may be NULL (defaults).  Allocates the pool and the streams on the
+ * current device. */
+int gbsort_server_create(const gbsort_server_config* cfg, gbsort_server** out);
+/* Drains every queued and running request, then frees everything. */
+void gbsort_server_destroy(gbsort_server* server);
+/* Queues one request; *ticket identifies it.  GBSORT_ERR_BUDGET when the
+ * request alone needs more device bytes than the pool holds. */
+int gbsort_server_submit(gbsort_server* server, const gbsort_request* req,
+                         uint64_t* ticket);
+/* GBSORT_ERR_NOT_READY while queued or running; otherwise the request's final
+ * status, after which the ticket is retired (a second call returns
+ * GBSORT_ERR_INVALID_ARGUMENT). */
+int gbsort_server_poll(gbsort_server* server, uint64_t ticket);
+/* As poll, waiting up to timeout_ns for the request to finish. */
+int gbsort_server_wait(gbsort_server* server, uint64_t ticket,
+                       uint64_t timeout_ns);
+/* Waits until nothing is queued or running (GBSORT_ERR_NOT_READY on timeout). */
+int gbsort_server_drain(gbsort_server* server, uint64_t timeout_ns);
+/* While paused, requests queue but no batch is launched. */
+int gbsort_server_pause(gbsort_server* server);
+int gbsort_server_resume(gbsort_server* server);
+int gbsort_server_stats_get(gbsort_server* server, gbsort_server_stats* out);
+int gbsort_server_stats_reset(gbsort_server* server);
+
+/* ------------------------------------------------------------------------ */
 /* Workspace status and bounded waits                                       */
 /* ------------------------------------------------------------------------ */
+
+/* Clears the control block (error word, tile counters) of a workspace laid
+ * out for (key type, value size, n) on `stream`.  Every sort clears it itself
+ * before it starts; this only forgets a recorded error. */
+int gbsort_workspace_reset(int key_type, size_t value_bytes, size_t n,
+                           void* d_workspace, void* stream);
 
 /* Synchronizes `stream`, then reads the error word the last sort on this
  * workspace left (GBSORT_OK or GBSORT_ERR_TIMEOUT).  Needs the n, key type and
