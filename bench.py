@@ -84,16 +84,20 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def committed_traffic(config: str):
-    """dram bytes per pass launch from a committed ncu summary, if any."""
+def committed_traffic(config: str, n: int):
+    """DRAM bytes (read + write) per pass launch from the committed ncu
+    capture of this configuration's pass kernel, scaled to n keys when the
+    capture ran a smaller case (traffic grows with the tiles processed)."""
     path = os.path.join(REPO, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            d = json.load(f)
-        e = d.get(config)
-        return None if e is None else e
+            e = json.load(f).get(config)
+        if not e:
+            return None, None
+        scaled = e["dram_bytes_per_launch"] * n / e["captured_n"]
+        return int(scaled), f"ncu capture at n={e['captured_n']} scaled to n={n} ({e['summary']})"
     except Exception:
-        return None
+        return None, None
 
 
 class ClockSampler:
@@ -317,14 +321,15 @@ def bench_gbsort(args, cfg, world, rank, local):
     pass_ms = statistics.mean(statistics.mean(p[1:]) for p in per_kernel)
     pass_bytes = n * 2 * (kbytes + vb)
     achieved = pass_bytes / (pass_ms / 1e3) / 1e9
-    traffic = committed_traffic(args.config)
+    traffic, traffic_src = committed_traffic(args.config, n)
     sort_bytes = n * (kbytes + passes * 2 * (kbytes + vb))
     mean_sort_ms = total_ms / args.steps
     roofline = {"bound": "hbm", "kernel": "onesweep_pass_kernel", "achieved": round(achieved, 1),
                 "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s", "algorithmic_bytes_per_launch": pass_bytes,
-                "mean_launch_ms": round(pass_ms, 4), "upsweep_ms": round(ups_ms, 4)}
+                "mean_launch_ms": round(pass_ms, 4), "upsweep_ms": round(ups_ms, 4),
+                "traffic_source": traffic_src}
     sort_roofline = {"bytes_per_key": kbytes + passes * 2 * (kbytes + vb), "achieved": round(
         sort_bytes / (mean_sort_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
         "frac": round(sort_bytes / (mean_sort_ms / 1e3) / 1e9 / hbm, 4)}
@@ -370,7 +375,7 @@ def bench_gbsort(args, cfg, world, rank, local):
 
     # e2e: host buffers through the C ABI, copies inside the timed region
     e2e = None
-    if rank == 0 or world > 1:
+    if (rank == 0 or world > 1) and args.e2e_steps > 0:
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
         hbytes = n * kbytes
         h_src = torch.empty(hbytes, dtype=torch.uint8, pin_memory=True)
@@ -808,12 +813,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cub", action="store_true", help="skip the CUB comparator")
+    ap.add_argument("--n", type=int, default=0,
+                    help="override the configuration's key count (a smaller case for profiling)")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="c5: Poisson arrival rate in requests/s (0: the configured fraction of measured capacity)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # timing rule: at least 3 warm-up steps
     world, rank, local = dist_init()
     cfg = CONFIGS[args.config]
+    if args.n > 0 and cfg["n"]:
+        cfg = dict(cfg, n=args.n, workload=cfg["workload"] + f" (n overridden to {args.n})")
     if args.impl == "reference":
         bench_reference(args, cfg, world, rank)
     elif cfg.get("serving"):
