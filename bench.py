@@ -452,8 +452,13 @@ def bench_batched(args, cfg, world, rank, local):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     kt, vb = cfg["key"], cfg["vb"]
-    sizes = gen.log_uniform_sizes(cfg["segments"], cfg["seg_log2"][0], cfg["seg_log2"][1], seed=2026 + rank)
-    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    # N GPUs: a global batch of N x segments, split by bytes (the same greedy
+    # assignment on every rank, no collective); each rank sorts its share
+    sizes_all = gen.log_uniform_sizes(cfg["segments"] * world, cfg["seg_log2"][0], cfg["seg_log2"][1], seed=2026)
+    off_all = np.concatenate([[0], np.cumsum(sizes_all)]).astype(np.uint64)
+    owner, rank_bytes = gbsort.partition_segments(off_all, world, KEY_BYTES[kt], vb)
+    off, mine = gbsort.shard_offsets(off_all, owner, rank)
+    sizes = sizes_all[mine]
     n = int(off[-1])
     keys = torch.empty(n, dtype=torch.int32, device=dev)
     vals = torch.empty(n, dtype=torch.int32, device=dev)
@@ -502,7 +507,7 @@ def bench_batched(args, cfg, world, rank, local):
         raise RuntimeError(f"batched run reported {gbsort.status_string(st)}")
     ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = max_over_ranks(world, sum(ms))
-    value = world * steps * n / (total_ms / 1e3) / 1e9
+    value = steps * int(off_all[-1]) / (total_ms / 1e3) / 1e9  # every rank's keys / the slowest rank's time
 
     # device-side check of the last batch: every segment ascending, and each
     # (key, value) pair is an input pair (values are original indices)
@@ -548,6 +553,8 @@ def bench_batched(args, cfg, world, rank, local):
         "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": kt, "data": "synthetic",
         "config": {"workload": cfg["workload"], "n_keys": n, "segments": len(sizes), "value_bytes": vb,
+                   "sharding": {"global_segments": len(sizes_all), "ranks": world,
+                                "rank_bytes": [int(x) for x in rank_bytes]} if world > 1 else None,
                    "paths": {k: info[k] for k in ("cta_small4_segments", "cta_small_segments",
                                                   "cta_large_segments", "onesweep_segments", "onesweep_tiles",
                                                   "keys_in_cta", "keys_in_onesweep")},

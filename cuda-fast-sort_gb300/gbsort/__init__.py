@@ -491,3 +491,47 @@ def workspace_reset(key_type, n: int, workspace, value_bytes: int = 0, stream=No
     _declare_server(lib())
     _check(lib().gbsort_workspace_reset(key_type_id(key_type), value_bytes, n, _ptr(workspace), _stream(stream)),
            "workspace reset")
+
+
+# ---- multi-GPU sharding (host only) -----------------------------------------
+
+def partition_weights(weights, world: int):
+    """Bytes-balanced owner rank of every item (gbsort_partition_weights);
+    returns (owner int32 array, per-rank load uint64 array)."""
+    import numpy as np
+
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.uint64))
+    owner = np.empty(len(w), dtype=np.int32)
+    load = np.zeros(max(1, world), dtype=np.uint64)
+    f = lib().gbsort_partition_weights
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    _check(f(w.ctypes.data, len(w), world, owner.ctypes.data, load.ctypes.data), "partition")
+    return owner, load[:world]
+
+
+def partition_segments(offsets, world: int, key_bytes: int, value_bytes: int = 0):
+    """Owner rank of every segment of a batched sort, balanced by bytes."""
+    import numpy as np
+
+    off, _ = _offsets_array(offsets)
+    owner = np.empty(max(0, len(off) - 1), dtype=np.int32)
+    load = np.zeros(max(1, world), dtype=np.uint64)
+    f = lib().gbsort_partition_segments
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t,
+                  ctypes.c_void_p, ctypes.c_void_p]
+    _check(f(off.ctypes.data, len(owner), world, key_bytes, value_bytes, owner.ctypes.data, load.ctypes.data),
+           "partition")
+    return owner, load[:world]
+
+
+def shard_offsets(offsets, owner, rank: int):
+    """Offsets of the compacted batch holding only `rank`'s segments (in
+    their original order) and the indices of those segments."""
+    import numpy as np
+
+    off = np.asarray(offsets, dtype=np.uint64)
+    mine = np.nonzero(np.asarray(owner) == rank)[0]
+    sizes = (off[1:] - off[:-1])[mine]
+    return np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64), mine

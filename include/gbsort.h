@@ -325,6 +325,27 @@ int gbsort_server_stats_get(gbsort_server* server, gbsort_server_stats* out);
 int gbsort_server_stats_reset(gbsort_server* server);
 
 /* ------------------------------------------------------------------------ */
+/* Multi-GPU sharding of independent work — no counterpart in the reference */
+/* (one GPU).  Segments and requests are independent, so they are split     */
+/* across ranks by bytes with no collective and no data exchange: every     */
+/* rank computes the same assignment from the same host sizes and sorts only */
+/* what it owns.  Greedy longest-processing-time: items by decreasing       */
+/* weight, each to the least-loaded rank (ties: lowest index, lowest rank). */
+/* Host only; needs no GPU.                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* owner_out[i] = rank of item i (num_items entries); rank_load_out (may be
+ * NULL) receives the total weight per rank (world entries). */
+int gbsort_partition_weights(const uint64_t* weights, size_t num_items,
+                             int world, int32_t* owner_out,
+                             uint64_t* rank_load_out);
+/* Same over the segments of a batched sort: weight of segment i =
+ * (offsets[i+1] - offsets[i]) * (key_bytes + value_bytes). */
+int gbsort_partition_segments(const uint64_t* h_offsets, size_t num_segments,
+                              int world, size_t key_bytes, size_t value_bytes,
+                              int32_t* owner_out, uint64_t* rank_bytes_out);
+
+/* ------------------------------------------------------------------------ */
 /* Workspace status and bounded waits                                       */
 /* ------------------------------------------------------------------------ */
 
