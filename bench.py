@@ -68,6 +68,15 @@ CONFIGS = {
                         "64 GiB device pool"),
 }
 KEY_BYTES = {"u32": 4, "f32": 4, "u64": 8, "u128": 16}
+PLAIN_METRIC = "sort throughput (Gkeys/s) and HBM roofline fraction"
+BATCHED_METRIC = "batched segmented sort throughput (Gkeys/s)"
+SERVING_METRIC = "serving throughput (Gkeys/s) under continuous batching, p50/p99 latency at load"
+
+
+def metric_of(cfg) -> str:
+    if cfg.get("serving"):
+        return SERVING_METRIC
+    return BATCHED_METRIC if "segments" in cfg else PLAIN_METRIC
 FALLBACK_HBM_GBS = 6800.0
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -212,8 +221,10 @@ def bench_reference(args, cfg, world, rank):
     import _oracle
 
     oracle = _oracle.load()
+    if "segments" in cfg or cfg.get("serving"):
+        return bench_reference_items(args, cfg, world, oracle, cores)
     # size the per-step sample so the whole run stays within ~2 minutes
-    n_cfg = cfg["n"] or (1 << 29)  # batched: the workload's total keys
+    n_cfg = cfg["n"]
     probe_n = min(n_cfg, 1 << 22)
     probe = cpu_sample_bits(cfg, probe_n, seed=6)
     t0 = time.perf_counter()
@@ -233,11 +244,65 @@ def bench_reference(args, cfg, world, rank):
     value = n_sample / statistics.mean(times) / 1e9
     sample = f"{n_sample} keys of the same distribution per step (libstdc++ parallel stable_sort of twiddled keys)"
     line = {
-        "impl": "reference", "metric": "sort throughput", "value": round(value, 4), "unit": "Gkeys/s",
+        "impl": "reference", "metric": metric_of(cfg), "value": round(value, 4), "unit": "Gkeys/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * statistics.mean(times), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": cfg["key"], "data": "synthetic",
         "config": {"workload": cfg["workload"], "sample_keys": n_sample, "flush": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_reference_items(args, cfg, world, oracle, cores):
+    """Reference arm of the batched and serving configurations: the oracle
+    sorts a bounded sample of the workload's independent items (segments or
+    requests, drawn from the same distribution) one after another, each with
+    every host core."""
+    import numpy as np
+
+    from gbsort import gen
+
+    rng = np.random.default_rng(4040)
+    items = []
+    if "segments" in cfg:
+        sizes = gen.log_uniform_sizes(cfg["segments"], cfg["seg_log2"][0], cfg["seg_log2"][1], seed=2026)
+        items = [(cfg["key"], int(m), cfg["vb"]) for m in sizes]
+    else:
+        lo, hi = cfg["size_log2"]
+        for _ in range(4096):
+            kt = ("u32", "u64", "f32")[int(rng.integers(3))]
+            items.append((kt, int(np.floor(2.0 ** rng.uniform(lo, hi))), 4 if rng.random() < 0.5 else 0))
+    rng.shuffle(items)
+    budget = 100.0 / max(1, args.steps + args.warmup)  # seconds per step
+    times, keys_done = [], []
+    pos = 0
+    for step in range(args.warmup + args.steps):
+        t_step, k_step = 0.0, 0
+        while t_step < budget and k_step < (1 << 27):
+            kt, m, vb = items[pos % len(items)]
+            pos += 1
+            raw = gen.generate(1 if kt == "f32" else 0, KEY_BYTES[kt], m, 100 + pos)
+            vals = np.arange(m, dtype=np.uint32) if vb else None
+            t0 = time.perf_counter()
+            oracle.sort(kt, raw, cfg["desc"], vals, threads=cores)
+            t_step += time.perf_counter() - t0
+            k_step += m
+        if step >= args.warmup:
+            times.append(t_step)
+            keys_done.append(k_step)
+    value = sum(keys_done) / sum(times) / 1e9
+    what = "segments" if "segments" in cfg else "requests"
+    sample = (f"{sum(keys_done) // max(1, len(keys_done))} keys per step in whole {what} of the workload's "
+              f"distribution, sorted one after another (libstdc++ parallel stable_sort of twiddled keys)")
+    line = {
+        "impl": "reference", "metric": metric_of(cfg), "value": round(value, 4), "unit": "Gkeys/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * statistics.mean(times), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": cfg["key"], "data": "synthetic",
+        "config": {"workload": cfg["workload"], "flush": "inputs larger than L2"},
         "cpu_baseline": {"value": round(value, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -416,7 +481,7 @@ def bench_gbsort(args, cfg, world, rank, local):
         return
     plan = gbsort.plan(kt, n, vb)
     line = {
-        "metric": "sort throughput (Gkeys/s) and HBM roofline fraction", "value": round(value, 3),
+        "metric": PLAIN_METRIC, "value": round(value, 3),
         "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": kt, "data": "synthetic",
@@ -549,7 +614,7 @@ def bench_batched(args, cfg, world, rank, local):
     if rank != 0:
         return
     line = {
-        "metric": "batched segmented sort throughput (Gkeys/s)", "value": round(value, 3), "unit": "Gkeys/s",
+        "metric": BATCHED_METRIC, "value": round(value, 3), "unit": "Gkeys/s",
         "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": kt, "data": "synthetic",
         "config": {"workload": cfg["workload"], "n_keys": n, "segments": len(sizes), "value_bytes": vb,
@@ -766,7 +831,7 @@ def bench_serving(args, cfg, world, rank, local):
     mean_keys = keys_cap / n_cap
     hbm, _ = peaks()
     line = {
-        "metric": "serving throughput (Gkeys/s) under continuous batching, p50/p99 latency at load",
+        "metric": SERVING_METRIC,
         "value": round(value, 3), "unit": "Gkeys/s", "n_gpus": world, "steps": n_cap, "warmup": args.warmup,
         "ms_per_step": round(1e3 * t_cap / n_cap, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32/u64/f32 keys, u32 values", "data": "synthetic",
