@@ -45,6 +45,12 @@ enum : uint32_t { ERRBIT_TIMEOUT = 1u, ERRBIT_BOUNDS = 2u };
 #define GBSORT_TILE_LOOKAHEAD 1
 #endif
 
+// Key-value passes: double-buffer only the keys and copy each tile's values
+// when the tile starts (1), or double-buffer keys and values (0).
+#ifndef GBSORT_LATE_VALUES
+#define GBSORT_LATE_VALUES 1
+#endif
+
 #ifndef GBSORT_LOOKBACK_PREFETCH
 #define GBSORT_LOOKBACK_PREFETCH 0
 #endif

@@ -154,21 +154,32 @@ struct PassGeom {
     static constexpr int IPW = 32 * IPT;
     // +16: a tile starting off the 16-byte grid is copied from the aligned
     // address below it and lands that many bytes into its region.
+    // LATE: only keys are double-buffered; each tile's values are copied into
+    // one value buffer when the tile starts (they land during its histogram
+    // and scan), so a tile costs 2K + V bytes of shared memory, not 2(K + V).
+    static constexpr bool LATE = GBSORT_LATE_VALUES != 0 && VB > 0;
     static constexpr size_t KEY_BYTES = size_t(TILE) * KB + 16;
-    static constexpr size_t VAL_OFF = (KEY_BYTES + 127) & ~size_t(127);
-    static constexpr size_t BUF_BYTES = (VAL_OFF + (VB ? size_t(TILE) * VB + 16 : 0) + 127) & ~size_t(127);
-    static constexpr size_t HIST_OFF = 2 * BUF_BYTES;             // u32 [WARPS][256]
+    static constexpr size_t VAL_BYTES = VB ? size_t(TILE) * VB + 16 : 0;
+    static constexpr size_t VAL_OFF = (KEY_BYTES + 127) & ~size_t(127);  // values inside a buffer (not LATE)
+    static constexpr size_t BUF_BYTES = LATE ? VAL_OFF : (VAL_OFF + VAL_BYTES + 127) & ~size_t(127);
+    static constexpr size_t LATE_VAL_OFF = 2 * BUF_BYTES;         // the value buffer (LATE)
+    static constexpr size_t HIST_OFF = LATE ? LATE_VAL_OFF + ((VAL_BYTES + 127) & ~size_t(127))
+                                            : 2 * BUF_BYTES;     // u32 [WARPS][256]
     static constexpr size_t GEXCL_OFF = HIST_OFF + size_t(WARPS) * 256 * 4;  // u64 [256]
     static constexpr size_t BINB_OFF = GEXCL_OFF + 256 * 8;       // u64 [256]
     static constexpr size_t SCAN64_OFF = BINB_OFF + 256 * 8;      // u64 [8]
     static constexpr size_t SCAN32_OFF = SCAN64_OFF + 64;         // u32 [8]
-    static constexpr size_t MBAR_OFF = SCAN32_OFF + 64;           // u64 [2]
-    static constexpr size_t INFO_OFF = MBAR_OFF + 16;             // TileInfo [2]
+    static constexpr size_t MBAR_OFF = SCAN32_OFF + 64;           // u64 [3]: buffers 0, 1, values
+    static constexpr size_t INFO_OFF = MBAR_OFF + 32;             // TileInfo [2]
     static constexpr size_t BINB32_OFF = INFO_OFF + 2 * sizeof(TileInfo);  // u32 [256]
     static constexpr size_t MATCH_OFF = BINB32_OFF + 256 * 4;     // u32 [WARPS][256] when RANK_OR is used
     static constexpr size_t SMEM_BYTES = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);
     static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
     static_assert(TILE % 16 == 0, "plain tiles start on the 16-byte grid");
+    // offset of the values of the tile in buffer b
+    __host__ __device__ static constexpr size_t val_off(int b) {
+        return LATE ? LATE_VAL_OFF : size_t(b) * BUF_BYTES + VAL_OFF;
+    }
 };
 
 // One onesweep digit pass.  SEG = false: one array of n keys.  SEG = true:
@@ -210,6 +221,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
+        mbar_init(&mbar[2], 1);
         fence_mbar_init();
     }
     if constexpr (!SEG) {  // global exclusive digit offsets of this pass (once per CTA)
@@ -257,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         if (p.tma_keys) kbytes = (mk + ti.cnt * uint32_t(KB)) & ~15u;
         uint32_t mv = 0;
         uintptr_t va = 0;
-        if constexpr (PAIRS) {
+        if constexpr (PAIRS && !G::LATE) {
             va = reinterpret_cast<uintptr_t>(gvals_in + ti.base);
             mv = uint32_t(va & 15u);
             if (p.tma_vals) vbytes = (mv + ti.cnt * uint32_t(VB)) & ~15u;
@@ -265,7 +277,18 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         mbar_arrive_expect_tx(&mbar[slot], kbytes + vbytes);
         if (kbytes) bulk_copy_g2s(buf, reinterpret_cast<const void*>(ka - mk), kbytes, &mbar[slot], pol);
         if (PAIRS && vbytes)
-            bulk_copy_g2s(buf + G::VAL_OFF, reinterpret_cast<const void*>(va - mv), vbytes, &mbar[slot], pol);
+            bulk_copy_g2s(smem + G::val_off(slot), reinterpret_cast<const void*>(va - mv), vbytes, &mbar[slot],
+                          pol);
+    };
+    // LATE: the values of tile ti into the value buffer (barrier 2).
+    auto issue_vals = [&](const TileInfo& ti) {
+        const uintptr_t va = reinterpret_cast<uintptr_t>(gvals_in + ti.base);
+        const uint32_t mv = uint32_t(va & 15u);
+        const uint32_t vbytes = p.tma_vals ? ((mv + ti.cnt * uint32_t(VB)) & ~15u) : 0u;
+        mbar_arrive_expect_tx(&mbar[2], vbytes);
+        if (vbytes)
+            bulk_copy_g2s(smem + G::LATE_VAL_OFF, reinterpret_cast<const void*>(va - mv), vbytes, &mbar[2],
+                          l2_evict_first_policy());
     };
 
     // Tile ids come from the pass's atomic counter.  Thread 0 claims the next
@@ -288,12 +311,17 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     __syncthreads();
     TileInfo cur = info_slot[0];
     uint32_t parity = 0;  // bit s: parity of the next wait on buffer s
+    uint32_t vparity = 0;  // LATE: parity of the next wait on the value buffer
     uint32_t it = 0;
 
     bool next_issued = false;  // thread 0 only: a copy into the other buffer is in flight
     while (cur.id < T) {
         const int b = int(it & 1u);
         if (tid == 0) {
+            if constexpr (G::LATE) {  // this tile's values first: they are needed sooner
+                fence_proxy_async_smem();
+                issue_vals(cur);
+            }
 #if GBSORT_TILE_LOOKAHEAD >= 3
             const TileInfo ni = make_info(id_an, rec_an);
 #else  // claim the next tile only now: a CTA holds two claims at most
@@ -323,32 +351,34 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         const bool full = cnt == uint32_t(G::TILE);
         uint8_t* buf = smem + size_t(b) * G::BUF_BYTES;
         U* sk = reinterpret_cast<U*>(buf);                 // staging (aligned)
-        V* sv = reinterpret_cast<V*>(buf + G::VAL_OFF);
+        V* sv = reinterpret_cast<V*>(smem + G::val_off(b));
 
         // ---- load the tile into registers (warp-striped: stable rank order)
         U keys[IPT];
         V vals[PAIRS ? IPT : 1];
         const uint32_t mk = uint32_t(reinterpret_cast<uintptr_t>(gkeys_in + cur.base) & 15u);
         const uint32_t mv = PAIRS ? uint32_t(reinterpret_cast<uintptr_t>(gvals_in + cur.base) & 15u) : 0u;
-        const bool fast = full && mk == 0 && mv == 0 && p.tma_keys && (!PAIRS || p.tma_vals);
+        const bool fast =
+            full && mk == 0 && p.tma_keys && (!PAIRS || G::LATE || (mv == 0 && p.tma_vals));
         if (fast) {
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
                 const int j = warp * G::IPW + u * 32 + lane;
                 keys[u] = sk[j];
-                if constexpr (PAIRS) vals[u] = sv[j];
+                if constexpr (PAIRS && !G::LATE) vals[u] = sv[j];
             }
         } else {
             const uint32_t kbytes = p.tma_keys ? ((mk + cnt * uint32_t(KB)) & ~15u) : 0u;
             const uint32_t vbytes = (PAIRS && p.tma_vals) ? ((mv + cnt * uint32_t(VB)) & ~15u) : 0u;
             const U* ski = reinterpret_cast<const U*>(buf + mk);
-            const V* svi = reinterpret_cast<const V*>(buf + G::VAL_OFF + mv);
+            const V* svi = reinterpret_cast<const V*>(smem + G::val_off(b) + mv);
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
                 const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
                 if (j < cnt) {
                     keys[u] = (mk + (j + 1) * KB <= kbytes) ? ski[j] : gkeys_in[cur.base + j];
-                    if constexpr (PAIRS) vals[u] = (mv + (j + 1) * VB <= vbytes) ? svi[j] : gvals_in[cur.base + j];
+                    if constexpr (PAIRS && !G::LATE)
+                        vals[u] = (mv + (j + 1) * VB <= vbytes) ? svi[j] : gvals_in[cur.base + j];
                 } else {
                     keys[u] = U(~U(0));  // tail filler: sorts after every valid key
                 }
@@ -378,6 +408,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
             if (tid == 0) {
                 mbar_wait_bounded(&mbar[b], ((parity >> b) & 1u) ^ 1u, DRAIN_LIMIT_NS, p.err);
                 if (next_issued) mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
+                if constexpr (G::LATE) mbar_wait_bounded(&mbar[2], vparity, DRAIN_LIMIT_NS, p.err);
             }
             return;
         }
@@ -406,6 +437,26 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         if (tid < 256) {
 #pragma unroll
             for (int w = 0; w < G::WARPS; ++w) whist[w * 256 + tid] += excl;
+        }
+        // LATE: this tile's values, copied in since the tile started.  A copy
+        // that did not land in time leaves garbage values (positions are
+        // unaffected, the error word is set); the CTA stops after this tile.
+        bool vfail = false;
+        if constexpr (G::LATE) {
+            vfail = !mbar_wait_bounded(&mbar[2], vparity, p.wait_limit_ns, p.err);
+            vparity ^= 1u;
+            const uint32_t vbytes = p.tma_vals ? ((mv + cnt * uint32_t(VB)) & ~15u) : 0u;
+            const V* svi = reinterpret_cast<const V*>(smem + G::LATE_VAL_OFF + mv);
+            if (full && mv == 0 && p.tma_vals) {
+#pragma unroll
+                for (int u = 0; u < IPT; ++u) vals[u] = svi[warp * G::IPW + u * 32 + lane];
+            } else {
+#pragma unroll
+                for (int u = 0; u < IPT; ++u) {
+                    const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
+                    if (j < cnt) vals[u] = (mv + (j + 1) * VB <= vbytes) ? svi[j] : gvals_in[cur.base + j];
+                }
+            }
         }
         __syncthreads();
 
@@ -511,7 +562,18 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
             }
         }
         if (bad) atomicOr(p.err, ERRBIT_BOUNDS);
-        __syncthreads();
+        if constexpr (G::LATE) {
+            if (__syncthreads_or(vfail)) {  // a value copy ran out of time: drain and leave
+                if (tid == 0) {
+                    mbar_wait_bounded(&mbar[2], vparity ^ 1u, DRAIN_LIMIT_NS, p.err);
+                    if (next_issued)
+                        mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
+                }
+                return;
+            }
+        } else {
+            __syncthreads();
+        }
         cur = next_info;
         ++it;
     }

@@ -1,9 +1,9 @@
 // shapes.h — CTA geometry of the onesweep pass per (key bytes, value bytes).
 //
-// Chosen for GB300: 512 threads (16 warps; the first 256 threads own one
-// digit bin each), items per thread sized so two CTAs (two double-buffered
-// tiles each) fit in an SM's 228 KB of shared memory where possible and the
-// register file holds keys, values and ranks without spilling.
+// Chosen for GB300: items per thread sized so two CTAs fit in an SM's 228 KB
+// of shared memory where possible (two double-buffered key tiles, one value
+// tile, per-warp counters and match words per CTA) and the register file
+// holds keys, values and ranks without spilling.
 #pragma once
 
 namespace gbsort {
@@ -13,30 +13,31 @@ constexpr int HIST_THREADS = 1024;
 
 // Measured on a GB300 (pass kernel, bench.py configurations):
 //   4-byte keys only, 2^28:      384 x 24, 2 CTAs/SM  (67 Gkeys/s)
-//   f32 keys + u32 values, 2^28: 256 x 20, 2 CTAs/SM  (45 Gkeys/s)
-//   u64 keys + u64 values, 2^27: 256 x 10, 2 CTAs/SM  (12.9 Gkeys/s)
-//   u128 keys only, 2^26:        512 x 8,  1 CTA/SM   (5.9 Gkeys/s)
-// Other sizes follow by bytes per item within the same shared-memory budget
-// (two double-buffered tiles + per-warp counters and match words per CTA).
+//   f32 keys + u32 values, 2^28: 256 x 26, 2 CTAs/SM  (49 Gkeys/s)
+//   u64 keys + u64 values, 2^27: 256 x 14, 2 CTAs/SM  (15.0 Gkeys/s)
+//   u128 keys only, 2^26:        512 x 8,  1 CTA/SM   (6.1 Gkeys/s)
+// Tile bytes per key are 2K + V (only keys are double-buffered), so with
+// values the tile grows with 2(K + V) / (2K + V) over a layout that double
+// buffers both; other widths follow by bytes per item in the same budget.
 struct ShapeRow {
     int threads, ipt, min_ctas;
 };
 constexpr ShapeRow pass_shape_row(int kb, int vb) {
     if (kb <= 4) {
         if (vb == 0) return {384, 24, 2};
-        if (vb <= 4) return {256, 20, 2};
-        if (vb == 8) return {256, 12, 2};
-        return {256, 8, 2};
+        if (vb <= 4) return {256, 26, 2};
+        if (vb == 8) return {256, 20, 2};
+        return {256, 13, 2};
     }
     if (kb == 8) {
         if (vb == 0) return {256, 20, 2};
-        if (vb <= 4) return {256, 12, 2};
-        if (vb == 8) return {256, 10, 2};
-        return {256, 6, 2};
+        if (vb <= 4) return {256, 16, 2};
+        if (vb == 8) return {256, 14, 2};
+        return {256, 10, 2};
     }
     if (vb == 0) return {512, 8, 1};
-    if (vb <= 8) return {256, 6, 2};
-    return {256, 4, 2};
+    if (vb <= 8) return {256, 8, 2};
+    return {256, 6, 2};
 }
 
 template <int KB, int VB>
