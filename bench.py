@@ -383,7 +383,7 @@ def bench_gbsort(args, cfg, world, rank, local):
         per_kernel.append(gbsort.sort_timed(keys[r & 1], n, kt, ws, tb, values=vals[r & 1], value_bytes=vb,
                                             descending=desc, stream=stream))
     ups_ms = statistics.mean(p[0] for p in per_kernel)
-    pass_ms = statistics.mean(statistics.mean(p[1:]) for p in per_kernel)
+    pass_ms = statistics.mean(statistics.mean(p[1:1 + passes]) for p in per_kernel)
     pass_bytes = n * 2 * (kbytes + vb)
     achieved = pass_bytes / (pass_ms / 1e3) / 1e9
     traffic, traffic_src = committed_traffic(args.config, n)
@@ -498,8 +498,9 @@ def bench_gbsort(args, cfg, world, rank, local):
         "cpu_baseline": cpu,
         "comparators": {"cub": cub},
         "clocks": clk,
-        "gpu_launches": args.steps * (passes + 2 + (1 if vb else 0)),
-        "gpu_launches_note": "per step: generate (+values) + upsweep + one pass per key byte; plus one memset node",
+        "gpu_launches": args.steps * (plan.kernel_launches + 1 + (1 if vb else 0)),
+        "gpu_launches_note": "per step: generate (+values), then the sort's upsweep, one pass per key byte and "
+                             "the pass-skip fix-up copy (exits at once when no pass was skipped); plus one memset",
         "sorted_check": ok,
     }
     print(json.dumps(line), flush=True)

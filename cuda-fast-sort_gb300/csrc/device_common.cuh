@@ -199,7 +199,10 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
 //                and read it back (load/store pipe)
 // GBSORT_RANK_PATTERN lists the method per column of items (4 bits each,
 // column u uses nibble u % GBSORT_RANK_PATTERN_LEN), spreading the work.
-enum RankMethod : int { RANK_BALLOT = 0, RANK_MATCH = 1, RANK_OR = 2 };
+//   RANK_OR5:    OR into one of 32 words by the digit's high 5 bits (one
+//                word per bank: different words never conflict), then 3
+//                ballots on the low 3 bits
+enum RankMethod : int { RANK_BALLOT = 0, RANK_MATCH = 1, RANK_OR = 2, RANK_OR5 = 3 };
 #ifndef GBSORT_RANK_PATTERN
 #define GBSORT_RANK_PATTERN 0x2  // every column: shared-memory OR (fastest on GB300)
 #define GBSORT_RANK_PATTERN_LEN 1
@@ -209,7 +212,7 @@ __host__ __device__ constexpr int rank_method(int column) {
 }
 __host__ __device__ constexpr bool rank_uses_or(int ipt) {
     for (int u = 0; u < ipt; ++u)
-        if (rank_method(u) == RANK_OR) return true;
+        if (rank_method(u) == RANK_OR || rank_method(u) == RANK_OR5) return true;
     return false;
 }
 
@@ -234,10 +237,30 @@ __device__ __forceinline__ uint32_t match_or(uint32_t d, uint32_t* mb, int lane,
     return peers;
 }
 
+// `mb`: this warp's zeroed shared words (32 used, 32-word aligned); left
+// zeroed on return.
+__device__ __forceinline__ uint32_t match_or5(uint32_t d, uint32_t* mb, int lane, uint32_t lt) {
+    const uint32_t hi = d >> 3;
+    atomicOr(&mb[hi], 1u << lane);
+    uint32_t lo = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 3; ++bit) {
+        const uint32_t m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+        lo &= ((d >> bit) & 1u) ? m : ~m;
+    }
+    __syncwarp();
+    const uint32_t hi_peers = mb[hi];
+    __syncwarp();
+    if ((hi_peers & lt) == 0) mb[hi] = 0u;  // the high group's lowest lane clears
+    __syncwarp();
+    return hi_peers & lo;
+}
+
 template <int METHOD>
 __device__ __forceinline__ uint32_t warp_match_digit(uint32_t d, uint32_t* mb, int lane, uint32_t lt) {
     if constexpr (METHOD == RANK_MATCH) return __match_any_sync(0xffffffffu, d);
     else if constexpr (METHOD == RANK_OR) return match_or(d, mb, lane, lt);
+    else if constexpr (METHOD == RANK_OR5) return match_or5(d, mb, lane, lt);
     else return match_ballot(d);
 }
 

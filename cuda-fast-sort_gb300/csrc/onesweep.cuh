@@ -173,7 +173,8 @@ struct PassGeom {
     static constexpr size_t INFO_OFF = MBAR_OFF + 32;             // TileInfo [2]
     static constexpr size_t BINB32_OFF = INFO_OFF + 2 * sizeof(TileInfo);  // u32 [256]
     static constexpr size_t MATCH_OFF = BINB32_OFF + 256 * 4;     // u32 [WARPS][256] when RANK_OR is used
-    static constexpr size_t SMEM_BYTES = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);
+    static constexpr size_t SKIP_OFF = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);  // u32
+    static constexpr size_t SMEM_BYTES = SKIP_OFF + 16;
     static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
     static_assert(TILE % 16 == 0, "plain tiles start on the 16-byte grid");
     // offset of the values of the tile in buffer b
@@ -215,8 +216,39 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     const int pass = p.pass, kind = p.kind, desc = p.desc;
     const uint32_t epoch = uint32_t(pass);
     W* status = static_cast<W*>(p.status);
-    const U* gkeys_in = static_cast<const U*>(p.keys_in);
-    const V* gvals_in = static_cast<const V*>(p.vals_in);
+    const void* keys_in = p.keys_in;
+    void* keys_out = p.keys_out;
+    const void* vals_in = p.vals_in;
+    void* vals_out = p.vals_out;
+    int twiddle_load = p.twiddle_load, twiddle_store = p.twiddle_store;
+    if constexpr (!SEG) {
+        if (p.skip) {
+            // a pass is uniform when one digit holds all n keys
+            uint32_t* smask = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF);
+            if (tid == 0) *smask = 0u;
+            __syncthreads();
+            if (tid < 256) {
+                uint32_t m = 0;
+                for (int q = 0; q < p.passes; ++q) m |= uint32_t(p.gp_all[size_t(q) * 256 + tid] == n) << q;
+                if (m) atomicOr(smask, m);
+            }
+            __syncthreads();
+            const uint32_t uniform = *smask;
+            if ((uniform >> pass) & 1u) return;  // every CTA of this pass leaves: a no-op pass
+            const uint32_t all = (p.passes >= 32) ? 0xffffffffu : ((1u << p.passes) - 1u);
+            const int before = __popc(~uniform & ((1u << pass) - 1u));  // executed passes before this one
+            const int total = __popc(~uniform & all);
+            const bool from_b = ((p.start_alt + before) & 1) != 0;
+            keys_in = from_b ? p.keys_b : p.keys_a;
+            keys_out = from_b ? p.keys_a : p.keys_b;
+            vals_in = from_b ? p.vals_b : p.vals_a;
+            vals_out = from_b ? p.vals_a : p.vals_b;
+            twiddle_load = before == 0;
+            twiddle_store = before + 1 == total;
+        }
+    }
+    const U* gkeys_in = static_cast<const U*>(keys_in);
+    const V* gvals_in = static_cast<const V*>(vals_in);
 
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
@@ -384,7 +416,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
                 }
             }
         }
-        if (p.twiddle_load) {
+        if (twiddle_load) {
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
                 const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
@@ -517,8 +549,8 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         __syncthreads();
 
         // ---- coalesced write-out: thread-linear over the digit-sorted tile
-        U* okeys = static_cast<U*>(p.keys_out);
-        V* ovals = static_cast<V*>(p.vals_out);
+        U* okeys = static_cast<U*>(keys_out);
+        V* ovals = static_cast<V*>(vals_out);
         // Full tiles with 32-bit positions (n < 2^32) take a lean loop: one
         // shared load of the key, of its 32-bit base, one wide-address store.
         auto scatter32 = [&](auto twiddle_tag) {
@@ -541,10 +573,10 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
             }
         };
         if (full && n < 0xFFFFFFFFull) {
-            if (p.twiddle_store) scatter32(BoolTag<true>{});
+            if (twiddle_store) scatter32(BoolTag<true>{});
             else scatter32(BoolTag<false>{});
         } else {
-            const int tw_store = p.twiddle_store;
+            const int tw_store = twiddle_store;
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
                 const uint32_t i = uint32_t(u * THREADS + tid);

@@ -62,6 +62,48 @@ const KernelEntry* upsweep_entry(int kb) {
 namespace {
 
 std::atomic<uint64_t> g_wait_limit_ns{2000000000ull};
+// Uniform-digit pass skipping: on unless GBSORT_PASS_SKIP=0 or switched off.
+std::atomic<int> g_pass_skip{[] {
+    const char* v = std::getenv("GBSORT_PASS_SKIP");
+    return (v && v[0] == '0') ? 0 : 1;
+}()};
+
+// Copies `bytes` from src to dst with all threads of the grid (16-byte
+// vectors when both ends allow, else 4-byte words, else bytes).
+__device__ void grid_copy_bytes(void* dst, const void* src, uint64_t bytes) {
+    const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
+    uint64_t done = 0;
+    if ((a & 15u) == 0) {
+        const uint64_t v = bytes / 16;
+        for (uint64_t i = t; i < v; i += stride) static_cast<uint4*>(dst)[i] = static_cast<const uint4*>(src)[i];
+        done = v * 16;
+    } else if ((a & 3u) == 0) {
+        const uint64_t v = bytes / 4;
+        for (uint64_t i = t; i < v; i += stride)
+            static_cast<uint32_t*>(dst)[i] = static_cast<const uint32_t*>(src)[i];
+        done = v * 4;
+    }
+    for (uint64_t i = done + t; i < bytes; i += stride)
+        static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
+}
+
+// After uniform-pass skipping: an odd number of executed passes left the
+// result in the alternate buffer; copy it home.  Otherwise nothing to do.
+__global__ void __launch_bounds__(256) skip_fixup_kernel(FixupParams f) {
+    __shared__ uint32_t uniform;
+    if (threadIdx.x == 0) uniform = 0u;
+    __syncthreads();
+    uint32_t m = 0;
+    for (int q = 0; q < f.passes; ++q) m |= uint32_t(f.gp_all[size_t(q) * 256 + threadIdx.x] == f.n) << q;
+    if (m) atomicOr(&uniform, m);
+    __syncthreads();
+    const uint32_t all = (1u << f.passes) - 1u;
+    if ((__popc(~uniform & all) & 1) == 0) return;
+    grid_copy_bytes(f.keys_a, f.keys_b, f.key_bytes_total);
+    if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.vals_b, f.val_bytes_total);
+}
 thread_local std::string g_last_error;
 
 constexpr int MAX_DEVICES = 64;
@@ -237,7 +279,9 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     const bool odd = (plan.passes & 1) != 0;
     const int sms = device_sm_count();
 
-    const int nev = plan.passes + 2;
+    const bool skip = g_pass_skip.load(std::memory_order_relaxed) != 0;
+    const bool fixup = skip && !odd;  // odd pass counts start mirrored and always end at home
+    const int nev = plan.passes + 2 + (fixup ? 1 : 0);
     cudaEvent_t ev[20] = {};
     const bool timed = ms != nullptr;
     if (timed) {
@@ -307,10 +351,35 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         pp.tile_counter = counters + pass;
         pp.err = err_word;
         pp.wait_limit_ns = wait_limit_ns();
+        pp.skip = skip ? 1 : 0;
+        pp.passes = plan.passes;
+        pp.start_alt = odd ? 1 : 0;
+        pp.gp_all = gp;
+        pp.keys_a = d_keys;
+        pp.vals_a = d_values;
+        pp.keys_b = alt_keys;
+        pp.vals_b = alt_vals;
         void* args[] = {&pp};
         e = cudaLaunchKernel(plan.pass.fn, dim3(pass_ctas), dim3(plan.pass.threads), args, plan.pass.smem, stream);
         if (e != cudaSuccess) return fail("pass launch", e);
         if (timed) cudaEventRecord(ev[2 + pass], stream);
+    }
+    if (fixup) {
+        FixupParams fp{};
+        fp.gp_all = gp;
+        fp.n = plan.n;
+        fp.passes = plan.passes;
+        fp.keys_b = alt_keys;
+        fp.keys_a = d_keys;
+        fp.key_bytes_total = plan.n * uint64_t(plan.kb);
+        fp.vals_b = alt_vals;
+        fp.vals_a = d_values;
+        fp.val_bytes_total = plan.vb ? plan.n * uint64_t(plan.vb) : 0;
+        void* args[] = {&fp};
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(&skip_fixup_kernel), dim3(uint32_t(sms > 0 ? sms * 4 : 1)),
+                             dim3(256), args, 0, stream);
+        if (e != cudaSuccess) return fail("fixup launch", e);
+        if (timed) cudaEventRecord(ev[2 + plan.passes], stream);
     }
 
     if (timed) {
@@ -524,6 +593,9 @@ int gbsort_workspace_reset(int key_type, size_t value_bytes, size_t n, void* d_w
     return GBSORT_OK;
 }
 
+void gbsort_set_pass_skip(int enable) { g_pass_skip.store(enable ? 1 : 0, std::memory_order_relaxed); }
+int gbsort_get_pass_skip(void) { return g_pass_skip.load(std::memory_order_relaxed); }
+
 void gbsort_set_wait_limit_ns(uint64_t ns) { g_wait_limit_ns.store(ns, std::memory_order_relaxed); }
 uint64_t gbsort_get_wait_limit_ns(void) { return wait_limit_ns(); }
 
@@ -546,7 +618,7 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
         out->hist_ctas = uint32_t(sms);
     }
     out->status_word_bytes = plan.wide_status ? 8 : 4;
-    out->kernel_launches = uint32_t(plan.passes + 1);
+    out->kernel_launches = uint32_t(plan.passes + 1 + ((gbsort_get_pass_skip() && (plan.passes & 1) == 0) ? 1 : 0));
     out->workspace_bytes = plan.total_bytes;
     return GBSORT_OK;
 }

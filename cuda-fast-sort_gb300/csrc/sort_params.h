@@ -52,6 +52,32 @@ struct PassParams {
     // batched mode only
     const TileRec* tiles;       // [num_tiles]
     const uint32_t* seg_gofs;   // [segments][256] absolute output base of each digit, this pass
+    // Uniform-digit pass skipping (plain sort).  skip != 0: a pass whose digit
+    // is the same for all n keys is a no-op and exits; the kernel derives its
+    // buffers and twiddles from every pass's digit counts instead of taking
+    // keys_in/out, vals_in/out and twiddle_load/store from the host.
+    int skip;
+    int passes;
+    int start_alt;              // the data starts in the alternate buffer (mirrored)
+    const unsigned long long* gp_all;  // [passes][256]
+    void* keys_a;               // the caller's buffers
+    void* vals_a;
+    void* keys_b;               // the workspace's alternate buffers
+    void* vals_b;
+};
+
+// The copy home after uniform-pass skipping left an odd number of executed
+// passes (the result then sits in the alternate buffer).
+struct FixupParams {
+    const unsigned long long* gp_all;  // [passes][256]
+    uint64_t n;
+    int passes;
+    const void* keys_b;
+    void* keys_a;
+    uint64_t key_bytes_total;
+    const void* vals_b;
+    void* vals_a;
+    uint64_t val_bytes_total;
 };
 
 // Batched upsweep: one work item per chunk of one segment.

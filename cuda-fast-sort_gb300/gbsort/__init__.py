@@ -535,3 +535,17 @@ def shard_offsets(offsets, owner, rank: int):
     mine = np.nonzero(np.asarray(owner) == rank)[0]
     sizes = (off[1:] - off[:-1])[mine]
     return np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64), mine
+
+
+def set_pass_skip(enable: bool) -> None:
+    """Uniform-digit pass skipping on or off (process-wide; default on)."""
+    f = lib().gbsort_set_pass_skip
+    f.restype = None
+    f.argtypes = [ctypes.c_int]
+    f(int(enable))
+
+
+def get_pass_skip() -> bool:
+    f = lib().gbsort_get_pass_skip
+    f.restype = ctypes.c_int
+    return bool(f())

@@ -361,6 +361,18 @@ int gbsort_workspace_reset(int key_type, size_t value_bytes, size_t n,
 int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n,
                             void* d_workspace, void* stream);
 
+/* Uniform-digit pass skipping (default on; GBSORT_PASS_SKIP=0 in the
+ * environment turns it off at load).  A digit pass in which every key has
+ * the same digit leaves the order unchanged, so the sort runs only the other
+ * passes: each pass kernel reads the upsweep's digit counts on the device
+ * and exits when its digit is uniform, and a final copy kernel moves the
+ * result home when an odd number of passes ran.  Nothing synchronizes with
+ * the host.  The reference's optional form (EXIT_EARLY_OPT,
+ * include/rsort/detail/radix_kernel.cuh:298-323) copies the counts to the
+ * host first. */
+void gbsort_set_pass_skip(int enable);
+int gbsort_get_pass_skip(void);
+
 /* Upper bound, in nanoseconds, on any single device-side wait (lookback spin
  * or TMA barrier) of later launches.  Default 2e9 (2 s).  Process-wide. */
 void gbsort_set_wait_limit_ns(uint64_t ns);
@@ -399,7 +411,8 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n,
 /* Same as gbsort_sort_pairs (d_values may be NULL with value_bytes 0), but
  * records a CUDA event around every kernel on `stream` and, after
  * synchronizing, writes the per-kernel device milliseconds to ms_out:
- * ms_out[0] = histogram kernel, ms_out[1 + p] = digit pass p.  ms_cap is the
+ * ms_out[0] = histogram kernel, ms_out[1 + p] = digit pass p, and with pass
+ * skipping on and an even pass count P, ms_out[1 + P] = the fix-up copy.  ms_cap is the
  * capacity of ms_out; *n_ms receives the number of entries written. */
 int gbsort_sort_timed(int key_type, int descending, void* d_keys,
                       void* d_values, size_t value_bytes, void* d_workspace,
