@@ -222,27 +222,39 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
     void* vals_out = p.vals_out;
     int twiddle_load = p.twiddle_load, twiddle_store = p.twiddle_store;
     if constexpr (!SEG) {
-        if (p.skip) {
-            // a pass is uniform when one digit holds all n keys
-            uint32_t* smask = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF);
-            if (tid == 0) *smask = 0u;
-            __syncthreads();
-            if (tid < 256) {
-                uint32_t m = 0;
-                for (int q = 0; q < p.passes; ++q) m |= uint32_t(p.gp_all[size_t(q) * 256 + tid] == n) << q;
-                if (m) atomicOr(smask, m);
+        if (p.skip || p.copy_keys_in) {
+            uint32_t uniform = 0;
+            if (p.skip) {
+                // a pass is uniform when one digit holds all n keys
+                uint32_t* smask = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF);
+                if (tid == 0) *smask = 0u;
+                __syncthreads();
+                if (tid < 256) {
+                    uint32_t m = 0;
+                    for (int q = 0; q < p.passes; ++q) m |= uint32_t(p.gp_all[size_t(q) * 256 + tid] == n) << q;
+                    if (m) atomicOr(smask, m);
+                }
+                __syncthreads();
+                uniform = *smask;
+                if ((uniform >> pass) & 1u) return;  // every CTA of this pass leaves: a no-op pass
             }
-            __syncthreads();
-            const uint32_t uniform = *smask;
-            if ((uniform >> pass) & 1u) return;  // every CTA of this pass leaves: a no-op pass
             const uint32_t all = (p.passes >= 32) ? 0xffffffffu : ((1u << p.passes) - 1u);
             const int before = __popc(~uniform & ((1u << pass) - 1u));  // executed passes before this one
             const int total = __popc(~uniform & all);
-            const bool from_b = ((p.start_alt + before) & 1) != 0;
-            keys_in = from_b ? p.keys_b : p.keys_a;
-            keys_out = from_b ? p.keys_a : p.keys_b;
-            vals_in = from_b ? p.vals_b : p.vals_a;
-            vals_out = from_b ? p.vals_a : p.vals_b;
+            if (p.copy_keys_in) {
+                // the last executed pass writes the caller's output (a)
+                const bool to_a = ((total - 1 - before) & 1) == 0;
+                keys_out = to_a ? p.keys_a : p.keys_b;
+                vals_out = to_a ? p.vals_a : p.vals_b;
+                keys_in = before == 0 ? p.copy_keys_in : (to_a ? p.keys_b : p.keys_a);
+                vals_in = before == 0 ? p.copy_vals_in : (to_a ? p.vals_b : p.vals_a);
+            } else {
+                const bool from_b = ((p.start_alt + before) & 1) != 0;
+                keys_in = from_b ? p.keys_b : p.keys_a;
+                keys_out = from_b ? p.keys_a : p.keys_b;
+                vals_in = from_b ? p.vals_b : p.vals_a;
+                vals_out = from_b ? p.vals_a : p.vals_b;
+            }
             twiddle_load = before == 0;
             twiddle_store = before + 1 == total;
         }

@@ -56,8 +56,11 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan);
 
 // Enqueues one sort on `stream`.  `ms` (optional) receives per-kernel event
 // times after a stream sync: [upsweep, pass 0 .. pass P-1].
+// keys_src != nullptr: input-preserving sort, reads keys_src (and vals_src)
+// and leaves the result in d_keys (and d_values).
 int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values, void* d_workspace,
-                 cudaStream_t stream, float* ms, int ms_cap, int* n_ms);
+                 cudaStream_t stream, float* ms, int ms_cap, int* n_ms, const void* keys_src = nullptr,
+                 const void* vals_src = nullptr);
 
 // Device facts (cached per device).
 int device_sm_count();

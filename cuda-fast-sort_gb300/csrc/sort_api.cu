@@ -100,7 +100,14 @@ __global__ void __launch_bounds__(256) skip_fixup_kernel(FixupParams f) {
     if (m) atomicOr(&uniform, m);
     __syncthreads();
     const uint32_t all = (1u << f.passes) - 1u;
-    if ((__popc(~uniform & all) & 1) == 0) return;
+    const int executed = __popc(~uniform & all);
+    if (f.copy_keys_in) {  // input-preserving: only when no pass wrote the output
+        if (executed != 0) return;
+        grid_copy_bytes(f.keys_a, f.copy_keys_in, f.key_bytes_total);
+        if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.copy_vals_in, f.val_bytes_total);
+        return;
+    }
+    if ((executed & 1) == 0) return;
     grid_copy_bytes(f.keys_a, f.keys_b, f.key_bytes_total);
     if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.vals_b, f.val_bytes_total);
 }
@@ -259,7 +266,8 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
 }
 
 int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values, void* d_workspace,
-                 cudaStream_t stream, float* ms, int ms_cap, int* n_ms) {
+                 cudaStream_t stream, float* ms, int ms_cap, int* n_ms, const void* keys_src,
+                 const void* vals_src) {
     if (n_ms) *n_ms = 0;
     if (plan.n == 0) return GBSORT_OK;
     if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
@@ -276,11 +284,14 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     void* status = ws + plan.status_off;
     void* alt_keys = ws + plan.alt_keys_off;
     void* alt_vals = plan.vb ? ws + plan.alt_vals_off : nullptr;
-    const bool odd = (plan.passes & 1) != 0;
+    const bool copy = keys_src != nullptr;  // input-preserving: read keys_src/vals_src, write d_keys/d_values
+    const bool odd = !copy && (plan.passes & 1) != 0;
     const int sms = device_sm_count();
 
     const bool skip = g_pass_skip.load(std::memory_order_relaxed) != 0;
-    const bool fixup = skip && !odd;  // odd pass counts start mirrored and always end at home
+    // odd pass counts start mirrored and always end at home; an
+    // input-preserving sort needs the copy only when every pass was skipped
+    const bool fixup = skip && ((plan.passes & 1) == 0 || copy);
     const int nev = plan.passes + 2 + (fixup ? 1 : 0);
     cudaEvent_t ev[20] = {};
     const bool timed = ms != nullptr;
@@ -300,7 +311,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     if (e != cudaSuccess) return fail("memset control block", e);
 
     HistParams hp{};
-    hp.keys = d_keys;
+    hp.keys = copy ? keys_src : d_keys;
     hp.n = plan.n;
     hp.kind = plan.kind;
     hp.desc = descending;
@@ -308,7 +319,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     hp.status = status;
     hp.status_bytes = plan.status_bytes;
     hp.mirror_keys = odd ? alt_keys : nullptr;
-    hp.vals = d_values;
+    hp.vals = copy ? vals_src : d_values;
     hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
     hp.val_bytes_total = plan.n * uint64_t(plan.vb);
     const uint64_t hist_work = (plan.n * uint64_t(plan.kb) + (HIST_THREADS * 64ull) - 1) /
@@ -359,6 +370,8 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         pp.vals_a = d_values;
         pp.keys_b = alt_keys;
         pp.vals_b = alt_vals;
+        pp.copy_keys_in = copy ? keys_src : nullptr;
+        pp.copy_vals_in = copy ? vals_src : nullptr;
         void* args[] = {&pp};
         e = cudaLaunchKernel(plan.pass.fn, dim3(pass_ctas), dim3(plan.pass.threads), args, plan.pass.smem, stream);
         if (e != cudaSuccess) return fail("pass launch", e);
@@ -375,6 +388,8 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         fp.vals_b = alt_vals;
         fp.vals_a = d_values;
         fp.val_bytes_total = plan.vb ? plan.n * uint64_t(plan.vb) : 0;
+        fp.copy_keys_in = copy ? keys_src : nullptr;
+        fp.copy_vals_in = copy ? vals_src : nullptr;
         void* args[] = {&fp};
         e = cudaLaunchKernel(reinterpret_cast<const void*>(&skip_fixup_kernel), dim3(uint32_t(sms > 0 ? sms * 4 : 1)),
                              dim3(256), args, 0, stream);
@@ -444,9 +459,66 @@ int sort_common(int key_type, int descending, void* d_keys, void* d_values, size
                         static_cast<cudaStream_t>(stream), nullptr, 0, nullptr);
 }
 
+bool ranges_overlap(const void* a, const void* b, size_t bytes) {
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return bytes != 0 && x < y + bytes && y < x + bytes;
+}
+
+// Input-preserving form: keys_in/vals_in are only read, the result goes to
+// keys_out/vals_out.  Identical input and output buffers mean in place;
+// any other overlap is refused.
+int sort_copy_common(int key_type, int descending, const void* keys_in, void* keys_out, const void* vals_in,
+                     void* vals_out, size_t value_bytes, size_t* temp_bytes, void* d_workspace, size_t n,
+                     void* stream) {
+    int st = check_args(key_type, value_bytes, keys_out, vals_out, temp_bytes);
+    if (st != GBSORT_OK) return st;
+    Plan plan;
+    st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (d_workspace == nullptr) {
+        *temp_bytes = plan.total_bytes;
+        return GBSORT_OK;
+    }
+    if (n == 0) return GBSORT_OK;
+    if (keys_in == nullptr || keys_out == nullptr ||
+        (value_bytes != 0 && (vals_in == nullptr || vals_out == nullptr)))
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    const size_t kbytes = n * size_t(plan.kb), vbytes = n * value_bytes;
+    const bool keys_same = keys_in == keys_out, vals_same = value_bytes == 0 || vals_in == vals_out;
+    if (keys_same && vals_same)
+        return sort_common(key_type, descending, keys_out, vals_out, value_bytes, temp_bytes, d_workspace, n,
+                           stream);
+    if (ranges_overlap(keys_in, keys_out, kbytes) || (value_bytes && ranges_overlap(vals_in, vals_out, vbytes))) {
+        set_last_error_text("input and output buffers overlap (identical buffers sort in place)");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
+    if (!naturally_aligned(keys_in, size_t(plan.kb)) || !naturally_aligned(keys_out, size_t(plan.kb)) ||
+        !naturally_aligned(vals_in, value_bytes) || !naturally_aligned(vals_out, value_bytes)) {
+        set_last_error_text("keys and values must be aligned to their own size");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
+    if (*temp_bytes < plan.total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    return enqueue_sort(plan, descending ? 1 : 0, keys_out, value_bytes ? vals_out : nullptr, d_workspace,
+                        static_cast<cudaStream_t>(stream), nullptr, 0, nullptr, keys_in,
+                        value_bytes ? vals_in : nullptr);
+}
+
 }  // namespace
 
 extern "C" {
+
+int gbsort_sort_keys_copy(int key_type, int descending, const void* d_keys_in, void* d_keys_out,
+                          size_t* temp_bytes, void* d_workspace, size_t n, void* stream) {
+    return sort_copy_common(key_type, descending, d_keys_in, d_keys_out, nullptr, nullptr, 0, temp_bytes,
+                            d_workspace, n, stream);
+}
+
+int gbsort_sort_pairs_copy(int key_type, int descending, const void* d_keys_in, void* d_keys_out,
+                           const void* d_values_in, void* d_values_out, size_t value_bytes, size_t* temp_bytes,
+                           void* d_workspace, size_t n, void* stream) {
+    return sort_copy_common(key_type, descending, d_keys_in, d_keys_out, d_values_in, d_values_out, value_bytes,
+                            temp_bytes, d_workspace, n, stream);
+}
 
 size_t gbsort_key_bytes(int key_type) {
     static const size_t b[GBSORT_KEY_COUNT] = {1, 2, 4, 8, 16, 1, 2, 4, 8, 16, 4, 8, 16};

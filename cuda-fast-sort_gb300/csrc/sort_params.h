@@ -64,6 +64,11 @@ struct PassParams {
     void* vals_a;
     void* keys_b;               // the workspace's alternate buffers
     void* vals_b;
+    // Input-preserving sort: the first executed pass reads these, passes then
+    // alternate between the caller's output (keys_a/vals_a) and the alternate
+    // buffers so that the last one lands in the output.  nullptr: in place.
+    const void* copy_keys_in;
+    const void* copy_vals_in;
 };
 
 // The copy home after uniform-pass skipping left an odd number of executed
@@ -78,6 +83,9 @@ struct FixupParams {
     const void* vals_b;
     void* vals_a;
     uint64_t val_bytes_total;
+    // input-preserving sort: when no pass ran, copy these to the output
+    const void* copy_keys_in;
+    const void* copy_vals_in;
 };
 
 // Batched upsweep: one work item per chunk of one segment.

@@ -549,3 +549,62 @@ def get_pass_skip() -> bool:
     f = lib().gbsort_get_pass_skip
     f.restype = ctypes.c_int
     return bool(f())
+
+
+def sort_copy(keys_in, keys_out, n: int, key_type, workspace, workspace_bytes: int, *, values_in=None,
+              values_out=None, value_bytes: int = 0, descending: bool = False, stream=None) -> None:
+    """Input-preserving sort (gbsort_sort_keys_copy / gbsort_sort_pairs_copy):
+    reads keys_in (values_in), writes the sorted result to keys_out
+    (values_out)."""
+    l = lib()
+    vp, sz, i = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+    tb = ctypes.c_size_t(workspace_bytes)
+    kt = key_type_id(key_type)
+    if value_bytes:
+        f = l.gbsort_sort_pairs_copy
+        f.restype = i
+        f.argtypes = [i, i, vp, vp, vp, vp, sz, ctypes.POINTER(ctypes.c_size_t), vp, sz, vp]
+        st = f(kt, int(descending), _ptr(keys_in), _ptr(keys_out), _ptr(values_in), _ptr(values_out), value_bytes,
+               ctypes.byref(tb), _ptr(workspace), n, _stream(stream))
+    else:
+        f = l.gbsort_sort_keys_copy
+        f.restype = i
+        f.argtypes = [i, i, vp, vp, ctypes.POINTER(ctypes.c_size_t), vp, sz, vp]
+        st = f(kt, int(descending), _ptr(keys_in), _ptr(keys_out), ctypes.byref(tb), _ptr(workspace), n,
+               _stream(stream))
+    _check(st, "sort copy")
+
+
+# ---- device-side result checks ------------------------------------------------
+
+def check_order(keys, n: int, key_type, descending: bool = False, stream=None) -> int:
+    """Adjacent pairs out of order (0 for a sorted array)."""
+    f = lib().gbsort_check_order
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                  ctypes.POINTER(ctypes.c_uint64)]
+    out = ctypes.c_uint64(0)
+    _check(f(key_type_id(key_type), int(descending), _ptr(keys), n, _stream(stream), ctypes.byref(out)), "order")
+    return out.value
+
+
+def checksum(keys, n: int, key_type, stream=None) -> int:
+    """Order-independent checksum of the keys (equal for any permutation)."""
+    f = lib().gbsort_checksum
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+    out = ctypes.c_uint64(0)
+    _check(f(key_type_id(key_type), _ptr(keys), n, _stream(stream), ctypes.byref(out)), "checksum")
+    return out.value
+
+
+def check_pairs(keys_in, keys_out, index_values, value_bytes: int, n: int, key_type, stream=None) -> int:
+    """Output positions whose index value does not point at an equal input key."""
+    f = lib().gbsort_check_pairs
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+    out = ctypes.c_uint64(0)
+    _check(f(key_type_id(key_type), _ptr(keys_in), _ptr(keys_out), _ptr(index_values), value_bytes, n,
+             _stream(stream), ctypes.byref(out)), "pairs")
+    return out.value

@@ -103,6 +103,22 @@ int gbsort_sort_pairs(int key_type, int descending, void* d_keys,
                       void* d_values, size_t value_bytes, size_t* temp_bytes,
                       void* d_workspace, size_t n, void* stream);
 
+/* Input-preserving ("DoubleBuffer") forms, like the reference's CUB
+ * comparator (benchmark/cub_radix_double.cu:82-111): keys_in / values_in are
+ * only read and the sorted result is written to keys_out / values_out; the
+ * passes ping-pong between the output and the workspace, arranged on the
+ * device so the last one lands in the output (no extra copy).  Same size
+ * query and workspace size as the in-place form.  Identical input and output
+ * pointers sort in place; any other overlap is GBSORT_ERR_INVALID_ARGUMENT. */
+int gbsort_sort_keys_copy(int key_type, int descending, const void* d_keys_in,
+                          void* d_keys_out, size_t* temp_bytes,
+                          void* d_workspace, size_t n, void* stream);
+int gbsort_sort_pairs_copy(int key_type, int descending, const void* d_keys_in,
+                           void* d_keys_out, const void* d_values_in,
+                           void* d_values_out, size_t value_bytes,
+                           size_t* temp_bytes, void* d_workspace, size_t n,
+                           void* stream);
+
 /* Typed convenience entry points (same semantics as above). */
 #define GBSORT_DECLARE_TYPED(name)                                              \
     int gbsort_sort_##name(void* d_keys, size_t* temp_bytes, void* d_workspace, \
@@ -385,6 +401,25 @@ uint64_t gbsort_get_wait_limit_ns(void);
  * lookback without stalling any sort. */
 int gbsort_probe_wait_timeout(void* d_scratch, uint64_t limit_ns,
                               void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Result checks on the device (the reference's post-sort checks,           */
+/* benchmark/benchmark_sort.cuh:26-175: order, counts, pairs).  Each runs on */
+/* `stream`, synchronizes it and allocates 8 device bytes stream-ordered.   */
+/* ------------------------------------------------------------------------ */
+
+/* Adjacent pairs out of order, compared as the sort orders keys. */
+int gbsort_check_order(int key_type, int descending, const void* d_keys,
+                       size_t n, void* stream, uint64_t* violations);
+/* Order-independent 64-bit checksum of n keys: equal for any permutation. */
+int gbsort_checksum(int key_type, const void* d_keys, size_t n, void* stream,
+                    uint64_t* sum);
+/* Values that hold each key's original index (4 or 8 bytes): counts output
+ * positions i whose d_keys_in[index[i]] differs from d_keys_out[i]. */
+int gbsort_check_pairs(int key_type, const void* d_keys_in,
+                       const void* d_keys_out, const void* d_index_values,
+                       size_t value_bytes, size_t n, void* stream,
+                       uint64_t* violations);
 
 /* ------------------------------------------------------------------------ */
 /* Introspection used by the benchmark                                      */
