@@ -173,7 +173,8 @@ struct PassGeom {
     static constexpr size_t INFO_OFF = MBAR_OFF + 32;             // TileInfo [2]
     static constexpr size_t BINB32_OFF = INFO_OFF + 2 * sizeof(TileInfo);  // u32 [256]
     static constexpr size_t MATCH_OFF = BINB32_OFF + 256 * 4;     // u32 [WARPS][256] when RANK_OR is used
-    static constexpr size_t SKIP_OFF = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);  // u32
+    // u32 [4]: [0] uniform-pass mask (prologue), [1] this tile is uniform
+    static constexpr size_t SKIP_OFF = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);
     static constexpr size_t SMEM_BYTES = SKIP_OFF + 16;
     static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
     static_assert(TILE % 16 == 0, "plain tiles start on the 16-byte grid");
@@ -438,6 +439,8 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
 
         // ---- warp-private digit histograms (early counts)
         uint32_t* wh = whist + warp * 256;
+        uint32_t* uniform_tile = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF) + 1;
+        if (tid == 0) *uniform_tile = 0u;  // the last tile's readers passed its final barrier
 #pragma unroll
         for (int i = lane; i < 256; i += 32) wh[i] = 0u;
         __syncwarp();
@@ -470,6 +473,7 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
                 total += c;
             }
             valid_total = total - ((tid == 255) ? (uint32_t(G::TILE) - cnt) : 0u);
+            if (GBSORT_TILE_SHORTCUT && total == uint32_t(G::TILE)) *uniform_tile = 1u;  // all keys: this digit
             st_relaxed(status + size_t(cur.id) * 256 + tid,
                        Codec::pack(cur.first ? Codec::GLOBAL : Codec::PARTIAL, epoch, valid_total));
 #if GBSORT_LOOKBACK_PREFETCH
@@ -507,22 +511,29 @@ __global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep
         // ---- rank: warp match + popc + one shared atomic per digit group;
         // the group's base comes from the leader (lowest lane) by shuffle.
         uint32_t rank[IPT];
-        const uint32_t lt = lanemask_lt();
-        uint32_t* mb = match_scratch + warp * 256;
-        StaticFor<0, IPT>::run([&](auto uc) {
-            constexpr int u = decltype(uc)::value;
-            const uint32_t d = digit_of(keys[u], pass);
-            const uint32_t peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
-            const uint32_t below = __popc(peers & lt);
+        if (GBSORT_TILE_SHORTCUT && *uniform_tile) {
+            // Block-level short-circuit: one digit holds the whole tile, so
+            // the stable order is the input order.
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) rank[u] = uint32_t(warp * G::IPW + u * 32 + lane);
+        } else {
+            const uint32_t lt = lanemask_lt();
+            uint32_t* mb = match_scratch + warp * 256;
+            StaticFor<0, IPT>::run([&](auto uc) {
+                constexpr int u = decltype(uc)::value;
+                const uint32_t d = digit_of(keys[u], pass);
+                const uint32_t peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
+                const uint32_t below = __popc(peers & lt);
 #if GBSORT_RANK_LEADER_BRANCH
-            uint32_t old = 0;
-            if (below == 0) old = atomicAdd(&wh[d], uint32_t(__popc(peers)));
+                uint32_t old = 0;
+                if (below == 0) old = atomicAdd(&wh[d], uint32_t(__popc(peers)));
 #else
-            // every lane issues the atomic, non-leaders add 0: no divergence
-            const uint32_t old = atomicAdd(&wh[d], below == 0 ? uint32_t(__popc(peers)) : 0u);
+                // every lane issues the atomic, non-leaders add 0: no divergence
+                const uint32_t old = atomicAdd(&wh[d], below == 0 ? uint32_t(__popc(peers)) : 0u);
 #endif
-            rank[u] = __shfl_sync(0xffffffffu, old, __ffs(peers) - 1) + below;
-        });
+                rank[u] = __shfl_sync(0xffffffffu, old, __ffs(peers) - 1) + below;
+            });
+        }
 
         // ---- stage at rank: every thread read its input before the first
         // barrier of this tile, so the buffer is free; keys/ranks die here,
