@@ -62,7 +62,7 @@ CONFIGS = {
                workload="batched: 4096 independent u32-key/u32-value sorts, segment lengths log-uniform in "
                         "[2^8, 2^20] (seeded), keys uniform 32-bit, ascending, one batched run per step"),
     "c5": dict(key="mixed", n=0, dist=0, vb=4, desc=False, serving=True, size_log2=(10, 24), pool=64 << 30,
-               streams=3, load=0.7,
+               streams=6, load=0.7,
                workload="serving: Poisson arrivals, request sizes log-uniform in [2^10, 2^24], key type u32 / u64 / "
                         "f32 with equal probability, 50% carry u32 values, ascending, host pinned buffers, "
                         "64 GiB device pool"),
@@ -745,6 +745,8 @@ def bench_serving(args, cfg, world, rank, local):
     plan_checks(reqs, "cap")
     keys_cap = sum(r[1] for r in reqs)
     bytes_in = sum(r[1] * (KEY_BYTES[r[0]] + (4 if r[2] else 0)) for r in reqs)
+    sort_bytes = sum(r[1] * (KEY_BYTES[r[0]] + KEY_BYTES[r[0]] * 2 * (KEY_BYTES[r[0]] + (4 if r[2] else 0)))
+                     for r in reqs)
     srv.reset_stats()
     clock = ClockSampler(local)
     barrier(world)
@@ -865,8 +867,17 @@ def bench_serving(args, cfg, world, rank, local):
         "e2e": {"value": round(value, 3), "unit": "Gkeys/s", "h2d_bytes_per_step": int(bytes_in / n_cap),
                 "d2h_bytes_per_step": int(bytes_in / n_cap),
                 "api": "gbsort_server_submit / drain with pinned HOST buffers (value is already end to end)"},
-        "roofline": {"bound": "hbm", "note": "the server's kernels are the batched sort's; host link bytes in "
-                                             "capacity.link_gbs", "peak": hbm, "unit": "GB/s"},
+        "roofline": {"bound": "hbm", "kernel": "batched sort (onesweep_pass_kernel over the batch's tile list)",
+                     "achieved": round(sort_bytes / max(cap_stats["sort_seconds"], 1e-9) / 1e9, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(sort_bytes / max(cap_stats["sort_seconds"], 1e-9) / 1e9 / hbm, 4),
+                     "traffic": None, "algorithmic_bytes": sort_bytes,
+                     "note": "K + P*2*(K+V) bytes per key over the batches' summed sort time (CUDA events on the "
+                             "sort stream); the request mix is bound by the host link, see link_roofline"},
+        "link_roofline": {"achieved": round(2 * bytes_in / t_cap / 1e9, 1), "peak": link.get("bidir_gbs"),
+                          "unit": "GB/s", "frac": round(2 * bytes_in / t_cap / 1e9 / max(link.get("bidir_gbs", 1), 1e-9),
+                                                        4),
+                          "note": "host<->device bytes of the capacity phase over its wall time, against pinned "
+                                  "copies in both directions at once"},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": cap_stats["kernel_launches"],

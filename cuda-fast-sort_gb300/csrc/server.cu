@@ -521,7 +521,7 @@ int gbsort_server_create(const gbsort_server_config* cfg, gbsort_server** out) {
     auto s = std::make_unique<gbsort_server>();
     if (cfg) s->cfg = *cfg;
     if (s->cfg.pool_bytes == 0) s->cfg.pool_bytes = uint64_t(64) << 30;
-    if (s->cfg.streams == 0) s->cfg.streams = 3;
+    if (s->cfg.streams == 0) s->cfg.streams = 6;
     if (s->cfg.streams > 16) return GBSORT_ERR_INVALID_ARGUMENT;
     if (s->cfg.max_batch_keys == 0) s->cfg.max_batch_keys = uint64_t(1) << 26;
     if (s->cfg.max_batch_requests == 0) s->cfg.max_batch_requests = 4096;

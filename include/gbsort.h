@@ -278,7 +278,7 @@ typedef struct gbsort_server gbsort_server;
 
 typedef struct gbsort_server_config {
     uint64_t pool_bytes;      /* device pool = admission budget (0: 64 GiB)  */
-    uint32_t streams;         /* batches in flight (0: 3)                    */
+    uint32_t streams;         /* batches in flight (0: 6)                    */
     uint32_t paused;          /* start paused (see gbsort_server_resume)     */
     uint64_t max_batch_keys;  /* keys coalesced into one launch (0: 2^26)    */
     uint64_t max_batch_requests; /* requests per launch (0: 4096)            */
