@@ -557,6 +557,7 @@ def bench_batched(args, cfg, world, rank, local):
         raise RuntimeError("batched warm-up reported an error")
     steps = max(1, min(args.steps, 40))
     ev = []
+    clocks = ClockSampler(local) if rank == 0 else None
     barrier(world)
     torch.cuda.synchronize()
     for i in range(steps):
@@ -568,6 +569,7 @@ def bench_batched(args, cfg, world, rank, local):
         ev.append((a, b))
     torch.cuda.synchronize()
     barrier(world)
+    clk = clocks.stop() if clocks else None
     st = plan.status(stream=stream)
     if st != gbsort.OK:
         raise RuntimeError(f"batched run reported {gbsort.status_string(st)}")
@@ -609,6 +611,57 @@ def bench_batched(args, cfg, world, rank, local):
         loop_ms.append(a.elapsed_time(b))
     loop_value = n / (min(loop_ms) / 1e3) / 1e9
 
+    # e2e: the batch arrives in pinned host memory and goes back there; the
+    # copies and the replayed batched run are inside the timed region
+    e2e = None
+    if args.e2e_steps > 0:
+        hk = torch.empty(n * 4, dtype=torch.uint8, pin_memory=True)
+        hv = torch.empty(n * vb, dtype=torch.uint8, pin_memory=True)
+        prepare(777)
+        torch.cuda.synchronize()
+        hk.copy_(keys.view(torch.uint8))
+        hv.copy_(vals.view(torch.uint8))
+        e2e_t = []
+        for _ in range(min(args.e2e_steps, 3) + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with torch.cuda.stream(stream):
+                keys.view(torch.uint8).copy_(hk, non_blocking=True)
+                vals.view(torch.uint8).copy_(hv, non_blocking=True)
+                plan.run(stream=stream)
+                hk.copy_(keys.view(torch.uint8), non_blocking=True)
+                hv.copy_(vals.view(torch.uint8), non_blocking=True)
+            stream.synchronize()
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_t = e2e_t[1:]
+        e2e = {"value": round(n / statistics.mean(e2e_t) / 1e9, 3), "unit": "Gkeys/s",
+               "h2d_bytes_per_step": n * (4 + vb), "d2h_bytes_per_step": n * (4 + vb), "steps": len(e2e_t),
+               "ms_per_step": round(1e3 * statistics.mean(e2e_t), 3),
+               "api": "SegmentedPlan.run (graph replay) between pinned host copies on the same stream"}
+        del hk, hv
+
+    # CPU oracle on a bounded sample of the segments (1 thread)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        import _oracle
+
+        oracle = _oracle.load()
+        spent, done_keys, count = 0.0, 0, 0
+        for s in np.random.default_rng(6).permutation(len(sizes)):
+            if spent > min(args.cpu_seconds, 15.0):
+                break
+            m = int(sizes[s])
+            raw = gen.generate(0, 4, m, 1000 + count)
+            t1 = time.perf_counter()
+            oracle.sort(kt, raw, False, np.arange(m, dtype=np.uint32))
+            spent += time.perf_counter() - t1
+            done_keys += m
+            count += 1
+        cpu = {"value": round(done_keys / spent / 1e9, 5), "unit": "Gkeys/s", "cores": 1, "kind": "port",
+               "sample": f"{count} segments of the workload ({done_keys} keys), std::stable_sort of twiddled keys "
+                         f"with u32 values, 1 thread"}
+
     hbm, peak_kind = peaks()
     algo_bytes = info["keys_in_cta"] * 2 * (4 + vb) + info["keys_in_onesweep"] * (4 + 4 * 2 * (4 + vb))
     mean_ms = total_ms / steps
@@ -628,10 +681,16 @@ def bench_batched(args, cfg, world, rank, local):
         "loop_baseline": {"value": round(loop_value, 3), "unit": "Gkeys/s", "ms": round(min(loop_ms), 3),
                           "impl": "gbsort_sort_pairs called once per segment (4096 calls), same GPU and data"},
         "speedup_vs_loop": round(value / loop_value, 2),
-        "sort_roofline": {"algorithmic_bytes": algo_bytes,
-                          "achieved": round(algo_bytes / (mean_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
-                          "frac": round(algo_bytes / (mean_ms / 1e3) / 1e9 / hbm, 4),
-                          "note": "CTA-sorted keys move 2*(K+V) bytes, onesweep keys K + P*2*(K+V)"},
+        "roofline": {"bound": "hbm", "kernel": "the batched run (segment upsweep, CTA sorts, onesweep passes over "
+                                                "the tile list) as one graph",
+                     "algorithmic_bytes": algo_bytes,
+                     "achieved": round(algo_bytes / (mean_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(algo_bytes / (mean_ms / 1e3) / 1e9 / hbm, 4), "traffic": None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "note": "CTA-sorted keys move 2*(K+V) bytes, onesweep keys K + P*2*(K+V); timed per replay"},
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clk,
         "autotune": {"seconds": round(tune_s, 1), "report": report.strip().splitlines()},
         "sorted_check": ok,
         "gpu_launches": steps * (info["kernel_launches"] + 2),
