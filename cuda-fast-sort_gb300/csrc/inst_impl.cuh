@@ -9,23 +9,34 @@
 
 namespace gbsort {
 
-template <int KB, int VB, class W, bool SEG>
+template <int KB, int VB, class W, bool SEG, class S = PassShape<KB, VB>>
 KernelEntry make_pass_entry() {
-    using S = PassShape<KB, VB>;
     using G = PassGeom<KB, VB, S::THREADS, S::IPT>;
-    return KernelEntry{reinterpret_cast<const void*>(&onesweep_pass_kernel<KB, VB, W, S::THREADS, S::IPT, SEG>),
-                       S::THREADS, S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
+    return KernelEntry{
+        reinterpret_cast<const void*>(&onesweep_pass_kernel<KB, VB, W, S::THREADS, S::IPT, SEG, S::MIN_CTAS>),
+        S::THREADS, S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
 }
+
+// [value size][0: 32-bit status, 1: 64-bit status, 2: small-n shape (32-bit)]
+template <int KB, int VB>
+struct PassRow {
+    KernelEntry e[3];
+    PassRow()
+        : e{make_pass_entry<KB, VB, uint32_t, false>(), make_pass_entry<KB, VB, uint64_t, false>(),
+            make_pass_entry<KB, VB, uint32_t, false, PassShapeSmall<KB, VB>>()} {}
+};
 
 template <int KB>
 const KernelEntry* pass_entries_for() {
-    static const KernelEntry e[6][2] = {
-        {make_pass_entry<KB, 0, uint32_t, false>(), make_pass_entry<KB, 0, uint64_t, false>()},
-        {make_pass_entry<KB, 1, uint32_t, false>(), make_pass_entry<KB, 1, uint64_t, false>()},
-        {make_pass_entry<KB, 2, uint32_t, false>(), make_pass_entry<KB, 2, uint64_t, false>()},
-        {make_pass_entry<KB, 4, uint32_t, false>(), make_pass_entry<KB, 4, uint64_t, false>()},
-        {make_pass_entry<KB, 8, uint32_t, false>(), make_pass_entry<KB, 8, uint64_t, false>()},
-        {make_pass_entry<KB, 16, uint32_t, false>(), make_pass_entry<KB, 16, uint64_t, false>()},
+    static const PassRow<KB, 0> r0;
+    static const PassRow<KB, 1> r1;
+    static const PassRow<KB, 2> r2;
+    static const PassRow<KB, 4> r4;
+    static const PassRow<KB, 8> r8;
+    static const PassRow<KB, 16> r16;
+    static const KernelEntry e[6][3] = {
+        {r0.e[0], r0.e[1], r0.e[2]},    {r1.e[0], r1.e[1], r1.e[2]},    {r2.e[0], r2.e[1], r2.e[2]},
+        {r4.e[0], r4.e[1], r4.e[2]},    {r8.e[0], r8.e[1], r8.e[2]},    {r16.e[0], r16.e[1], r16.e[2]},
     };
     return &e[0][0];
 }

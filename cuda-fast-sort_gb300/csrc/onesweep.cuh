@@ -189,8 +189,8 @@ struct PassGeom {
 // count), each segment's first tile publishes an inclusive prefix of its own
 // so lookback chains never cross segments, and digit bases come per segment
 // from p.seg_gofs.
-template <int KB, int VB, class W, int THREADS, int IPT, bool SEG>
-__global__ void __launch_bounds__(THREADS, PassShape<KB, VB>::MIN_CTAS) onesweep_pass_kernel(PassParams p) {
+template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int MIN_CTAS>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassParams p) {
     using U = typename KeyBits<KB>::U;
     using V = typename ValBits<VB>::V;
     using G = PassGeom<KB, VB, THREADS, IPT>;

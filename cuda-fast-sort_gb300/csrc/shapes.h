@@ -6,6 +6,8 @@
 // holds keys, values and ranks without spilling.
 #pragma once
 
+#include <cstdint>
+
 namespace gbsort {
 
 // Threads of the upsweep (global histogram) kernel.
@@ -39,6 +41,25 @@ constexpr ShapeRow pass_shape_row(int kb, int vb) {
     if (vb <= 8) return {256, 8, 2};
     return {256, 6, 2};
 }
+
+// Small inputs (n <= 2^22, the reference's "short" range): tiles of about half
+// the size at 256 threads and two CTAs per SM, so a short array still spreads
+// over the SMs (2^20 u32 keys: 114 tiles of 9216 keys leave SMs idle; 256 of
+// 4096 keys took 12.8 -> 14.2 Gkeys/s on GB300).
+constexpr ShapeRow pass_shape_small_row(int kb, int vb) {
+    if (kb <= 4) return {256, vb == 0 ? 16 : vb <= 4 ? 13 : vb == 8 ? 11 : 7, 2};
+    if (kb == 8) return {256, vb == 0 ? 11 : vb <= 4 ? 9 : vb == 8 ? 7 : 5, 2};
+    return {256, vb == 0 ? 8 : vb <= 8 ? 4 : 3, 2};
+}
+constexpr uint64_t SMALL_N_MAX = uint64_t(1) << 22;
+
+template <int KB, int VB>
+struct PassShapeSmall {
+    static constexpr int THREADS = pass_shape_small_row(KB, VB).threads;
+    static constexpr int IPT = pass_shape_small_row(KB, VB).ipt;
+    static constexpr int MIN_CTAS = pass_shape_small_row(KB, VB).min_ctas;
+    static constexpr int LOOKBACK_WINDOW = 4;
+};
 
 template <int KB, int VB>
 struct PassShape {

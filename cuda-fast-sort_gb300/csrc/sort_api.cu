@@ -244,7 +244,9 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     // value is < n (the last tile never publishes an inclusive prefix).
     const int value_bits32 = 30 - log2_exact(p.passes);
     p.wide_status = n > (uint64_t(1) << value_bits32);
-    p.pass = pass_entries(p.kb)[vi * 2 + (p.wide_status ? 1 : 0)];
+    // short arrays take the small-tile shape (always 32-bit status words)
+    const bool small = n <= SMALL_N_MAX && !p.wide_status;
+    p.pass = pass_entries(p.kb)[vi * 3 + (small ? 2 : p.wide_status ? 1 : 0)];
     p.upsweep = *upsweep_entry(p.kb);
     const uint64_t tiles = (n + uint64_t(p.pass.tile) - 1) / uint64_t(p.pass.tile);
     if (tiles > 0xFFFFFFFFull) return GBSORT_ERR_INVALID_ARGUMENT;
