@@ -165,7 +165,12 @@ struct PassGeom {
     static constexpr size_t LATE_VAL_OFF = 2 * BUF_BYTES;         // the value buffer (LATE)
     static constexpr size_t HIST_OFF = LATE ? LATE_VAL_OFF + ((VAL_BYTES + 127) & ~size_t(127))
                                             : 2 * BUF_BYTES;     // u32 [WARPS][256]
-    static constexpr size_t GEXCL_OFF = HIST_OFF + size_t(WARPS) * 256 * 4;  // u64 [256]
+    // HALF: per half-warp digit words [position:16 | lane mask:16] replace the
+    // per-warp counters and the per-warp match words
+    static constexpr bool HALF = GBSORT_RANK_HALF != 0;
+    static constexpr int HIST_ROWS = HALF ? 2 * WARPS : WARPS;
+    static constexpr int HPW = 16 * IPT;  // HALF: items per half-warp
+    static constexpr size_t GEXCL_OFF = HIST_OFF + size_t(HIST_ROWS) * 256 * 4;  // u64 [256]
     static constexpr size_t BINB_OFF = GEXCL_OFF + 256 * 8;       // u64 [256]
     static constexpr size_t SCAN64_OFF = BINB_OFF + 256 * 8;      // u64 [8]
     static constexpr size_t SCAN32_OFF = SCAN64_OFF + 64;         // u32 [8]
@@ -174,7 +179,8 @@ struct PassGeom {
     static constexpr size_t BINB32_OFF = INFO_OFF + 2 * sizeof(TileInfo);  // u32 [256]
     static constexpr size_t MATCH_OFF = BINB32_OFF + 256 * 4;     // u32 [WARPS][256] when RANK_OR is used
     // u32 [4]: [0] uniform-pass mask (prologue), [1] this tile is uniform
-    static constexpr size_t SKIP_OFF = MATCH_OFF + (rank_uses_or(IPT) ? size_t(WARPS) * 256 * 4 : 0);
+    static constexpr size_t SKIP_OFF = MATCH_OFF + ((!HALF && rank_uses_or(IPT)) ? size_t(WARPS) * 256 * 4 : 0);
+    static_assert(!HALF || TILE <= 65535, "HALF packs tile positions into 16 bits");
     static constexpr size_t SMEM_BYTES = SKIP_OFF + 16;
     static_assert(THREADS >= 256 && THREADS % 32 == 0, "bin owners need 256 threads");
     static_assert(TILE % 16 == 0, "plain tiles start on the 16-byte grid");
@@ -207,11 +213,20 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
     TileInfo* info_slot = reinterpret_cast<TileInfo*>(smem + G::INFO_OFF);
     uint32_t* binb32 = reinterpret_cast<uint32_t*>(smem + G::BINB32_OFF);
     uint32_t* match_scratch = reinterpret_cast<uint32_t*>(smem + G::MATCH_OFF);
-    if constexpr (rank_uses_or(IPT)) {
+    if constexpr (!G::HALF && rank_uses_or(IPT)) {
         for (int i = threadIdx.x; i < G::WARPS * 256; i += THREADS) match_scratch[i] = 0u;
     }
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // Tile position of item u of this thread: warp-striped (a warp's 32 lanes
+    // read 32 consecutive keys per column), or with HALF half-warp-striped
+    // (each half-warp owns a contiguous run, so its own counters rank stably).
+    auto item = [&](int u) -> uint32_t {
+        if constexpr (G::HALF)
+            return uint32_t((warp * 2 + (lane >> 4)) * G::HPW + u * 16 + (lane & 15));
+        else
+            return uint32_t(warp * G::IPW + u * 32 + lane);
+    };
     const uint32_t T = p.num_tiles;
     const uint64_t n = p.n;
     const int pass = p.pass, kind = p.kind, desc = p.desc;
@@ -408,7 +423,7 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
         if (fast) {
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
-                const int j = warp * G::IPW + u * 32 + lane;
+                const uint32_t j = item(u);
                 keys[u] = sk[j];
                 if constexpr (PAIRS && !G::LATE) vals[u] = sv[j];
             }
@@ -419,7 +434,7 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
             const V* svi = reinterpret_cast<const V*>(smem + G::val_off(b) + mv);
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
-                const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
+                const uint32_t j = item(u);
                 if (j < cnt) {
                     keys[u] = (mk + (j + 1) * KB <= kbytes) ? ski[j] : gkeys_in[cur.base + j];
                     if constexpr (PAIRS && !G::LATE)
@@ -432,20 +447,28 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
         if (twiddle_load) {
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
-                const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
+                const uint32_t j = item(u);
                 if (full || j < cnt) keys[u] = twiddle_in<U>(keys[u], kind, desc);
             }
         }
 
         // ---- warp-private digit histograms (early counts)
-        uint32_t* wh = whist + warp * 256;
+        // HALF: one row per half-warp, counts in the upper 16 bits
+        uint32_t* wh = whist + (G::HALF ? (warp * 2 + (lane >> 4)) : warp) * 256;
         uint32_t* uniform_tile = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF) + 1;
-        if (tid == 0) *uniform_tile = 0u;  // the last tile's readers passed its final barrier
+        if constexpr (GBSORT_TILE_SHORTCUT) {
+            if (tid == 0) *uniform_tile = 0u;  // the last tile's readers passed its final barrier
+        }
+        {
+            constexpr int ROW_WORDS = (G::HALF ? 2 : 1) * 256;
+            uint32_t* mine = whist + warp * ROW_WORDS;
 #pragma unroll
-        for (int i = lane; i < 256; i += 32) wh[i] = 0u;
+            for (int i = lane; i < ROW_WORDS; i += 32) mine[i] = 0u;
+        }
         __syncwarp();
+        constexpr uint32_t ONE = G::HALF ? (1u << 16) : 1u;
 #pragma unroll
-        for (int u = 0; u < IPT; ++u) atomicAdd(&wh[digit_of(keys[u], pass)], 1u);
+        for (int u = 0; u < IPT; ++u) atomicAdd(&wh[digit_of(keys[u], pass)], ONE);
         if (__syncthreads_or(!landed)) {
             // A bulk copy did not land within the limit (error word already
             // set).  Publish nothing computed from this buffer — garbage counts
@@ -467,9 +490,9 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
         W lb_pre[LBW];
         if (tid < 256) {
 #pragma unroll
-            for (int w = 0; w < G::WARPS; ++w) {
-                const uint32_t c = whist[w * 256 + tid];
-                whist[w * 256 + tid] = total;
+            for (int w = 0; w < G::HIST_ROWS; ++w) {
+                const uint32_t c = G::HALF ? (whist[w * 256 + tid] >> 16) : whist[w * 256 + tid];
+                whist[w * 256 + tid] = G::HALF ? (total << 16) : total;
                 total += c;
             }
             valid_total = total - ((tid == 255) ? (uint32_t(G::TILE) - cnt) : 0u);
@@ -484,7 +507,7 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
         const uint32_t excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
         if (tid < 256) {
 #pragma unroll
-            for (int w = 0; w < G::WARPS; ++w) whist[w * 256 + tid] += excl;
+            for (int w = 0; w < G::HIST_ROWS; ++w) whist[w * 256 + tid] += G::HALF ? (excl << 16) : excl;
         }
         // LATE: this tile's values, copied in since the tile started.  A copy
         // that did not land in time leaves garbage values (positions are
@@ -497,11 +520,11 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
             const V* svi = reinterpret_cast<const V*>(smem + G::LATE_VAL_OFF + mv);
             if (full && mv == 0 && p.tma_vals) {
 #pragma unroll
-                for (int u = 0; u < IPT; ++u) vals[u] = svi[warp * G::IPW + u * 32 + lane];
+                for (int u = 0; u < IPT; ++u) vals[u] = svi[item(u)];
             } else {
 #pragma unroll
                 for (int u = 0; u < IPT; ++u) {
-                    const uint32_t j = uint32_t(warp * G::IPW + u * 32 + lane);
+                    const uint32_t j = item(u);
                     if (j < cnt) vals[u] = (mv + (j + 1) * VB <= vbytes) ? svi[j] : gvals_in[cur.base + j];
                 }
             }
@@ -515,7 +538,27 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
             // Block-level short-circuit: one digit holds the whole tile, so
             // the stable order is the input order.
 #pragma unroll
-            for (int u = 0; u < IPT; ++u) rank[u] = uint32_t(warp * G::IPW + u * 32 + lane);
+            for (int u = 0; u < IPT; ++u) rank[u] = item(u);
+        } else if constexpr (G::HALF) {
+            // Packed half-warp words: one OR registers the lane in its digit's
+            // word, one read returns the peers (low 16 bits) and the group's
+            // next position (high 16 bits), and the group's lowest lane stores
+            // the advanced position with the mask cleared.
+            const uint32_t bit = 1u << (lane & 15);
+            const uint32_t lt16 = bit - 1u;
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) {
+                const uint32_t d = digit_of(keys[u], pass);
+                atomicOr(&wh[d], bit);
+                __syncwarp();
+                const uint32_t w = wh[d];
+                const uint32_t peers = w & 0xFFFFu;
+                const uint32_t below = __popc(peers & lt16);
+                rank[u] = (w >> 16) + below;
+                __syncwarp();
+                if (below == 0) wh[d] = (w & 0xFFFF0000u) + (uint32_t(__popc(peers)) << 16);
+                __syncwarp();
+            }
         } else {
             const uint32_t lt = lanemask_lt();
             uint32_t* mb = match_scratch + warp * 256;
