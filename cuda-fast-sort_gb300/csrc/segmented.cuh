@@ -218,9 +218,9 @@ __global__ void __launch_bounds__(THREADS) cta_sort_kernel(CtaSortParams p) {
                     total += c;
                 }
             }
-            uint32_t excl;
+            uint32_t excl, counted = 0;  // counted: items in live columns (fillers included)
             if constexpr (BINS == 256) {
-                excl = block_exclusive_scan_256<uint32_t>(total, scan32, nullptr);
+                excl = block_exclusive_scan_256<uint32_t>(total, scan32, &counted);
             } else {  // one warp scans the bins
                 uint32_t v = (tid < BINS) ? total : 0u;
 #pragma unroll
@@ -229,25 +229,32 @@ __global__ void __launch_bounds__(THREADS) cta_sort_kernel(CtaSortParams p) {
                     if (lane >= o) v += y;
                 }
                 excl = v - total;
+                counted = __shfl_sync(0xffffffffu, v, BINS - 1);
             }
             if (tid < BINS) {
 #pragma unroll
                 for (int w = 0; w < G::WARPS; ++w) whist[w * BINS + tid] += excl;
             }
-            __syncthreads();
+            // one digit holding the whole segment leaves its order unchanged
+            const bool uniform = __syncthreads_or(tid < BINS && total == counted);
             uint32_t rank[IPT];
-            StaticFor<0, IPT>::run([&](auto uc) {
-                constexpr int u = decltype(uc)::value;
-                if (!live(u)) return;
-                const uint32_t d = digit_bits<RBITS>(keys[u], pass);
-                uint32_t peers;
-                if constexpr (RBITS == 8) peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
-                else peers = match_ballot_bits<RBITS>(d);
-                const uint32_t below = __popc(peers & lt);
-                uint32_t old = 0;
-                if (below == 0) old = atomicAdd(&wh[d], uint32_t(__popc(peers)));
-                rank[u] = __shfl_sync(0xffffffffu, old, __ffs(peers) - 1) + below;
-            });
+            if (uniform) {
+#pragma unroll
+                for (int u = 0; u < IPT; ++u) rank[u] = uint32_t(warp * G::IPW + u * 32 + lane);
+            } else {
+                StaticFor<0, IPT>::run([&](auto uc) {
+                    constexpr int u = decltype(uc)::value;
+                    if (!live(u)) return;
+                    const uint32_t d = digit_bits<RBITS>(keys[u], pass);
+                    uint32_t peers;
+                    if constexpr (RBITS == 8) peers = warp_match_digit<rank_method(u)>(d, mb, lane, lt);
+                    else peers = match_ballot_bits<RBITS>(d);
+                    const uint32_t below = __popc(peers & lt);
+                    uint32_t old = 0;
+                    if (below == 0) old = atomicAdd(&wh[d], uint32_t(__popc(peers)));
+                    rank[u] = __shfl_sync(0xffffffffu, old, __ffs(peers) - 1) + below;
+                });
+            }
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
                 if (!live(u)) continue;

@@ -153,3 +153,25 @@ def test_autotuner_installs_paths_and_stays_exact(gb, cuda, oracle):
         gb.segmented_tuning_load(text)  # round trip
     finally:
         gb.set_segmented_path("u32", 4, -1, -1)
+
+
+@pytest.mark.parametrize("path", ["PATH_CTA_S", "PATH_CTA_S4", "PATH_CTA_L", "PATH_ONESWEEP"])
+@pytest.mark.parametrize("kt,mask", [("u32", 0x00000FFF), ("u64", 0x0000FF00FF0000FF), ("i16", 0x00FF)])
+def test_uniform_digits_per_segment(gb, cuda, oracle, path, kt, mask):
+    """Keys whose masked-out bytes are constant: those digit passes are
+    uniform inside every segment (the CTA sort short-circuits them)."""
+    rng = np.random.default_rng(31)
+    off = _layout(rng, 150, 2, 12, extras=(0, 1, 4095, 4096))
+    n = int(off[-1])
+    raw = raw_keys(kt, n, seed=17)
+    dt = raw.dtype
+    raw = ((raw.astype(np.uint64) & np.uint64(mask)) | np.uint64(0x0101010101010101 & ~mask)).astype(dt)
+    vals = np.arange(n, dtype=np.uint32)
+    vb = 4
+    try:
+        gb.set_segmented_path(kt, vb, -1, getattr(gb, path))
+        (r, v0, k, v), = _run(gb, cuda, kt, raw, vals, off, False)[0]
+    finally:
+        gb.set_segmented_path(kt, vb, -1, -1)
+    ek, ev = _expected(oracle, kt, raw, vals, off, False)
+    assert _eq(k, ek) and _eq(v, ev)
