@@ -237,24 +237,30 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
     const void* vals_in = p.vals_in;
     void* vals_out = p.vals_out;
     int twiddle_load = p.twiddle_load, twiddle_store = p.twiddle_store;
-    if constexpr (!SEG) {
+    {
         if (p.skip || p.copy_keys_in) {
             uint32_t uniform = 0;
+            const uint32_t all = (p.passes >= 32) ? 0xffffffffu : ((1u << p.passes) - 1u);
             if (p.skip) {
-                // a pass is uniform when one digit holds all n keys
-                uint32_t* smask = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF);
-                if (tid == 0) *smask = 0u;
-                __syncthreads();
-                if (tid < 256) {
-                    uint32_t m = 0;
-                    for (int q = 0; q < p.passes; ++q) m |= uint32_t(p.gp_all[size_t(q) * 256 + tid] == n) << q;
-                    if (m) atomicOr(smask, m);
+                if constexpr (SEG) {
+                    // the batched scan marked every pass whose digit varies in some segment
+                    uniform = ~ld_relaxed(p.nonuniform_mask) & all;
+                } else {
+                    // a pass is uniform when one digit holds all n keys
+                    uint32_t* smask = reinterpret_cast<uint32_t*>(smem + G::SKIP_OFF);
+                    if (tid == 0) *smask = 0u;
+                    __syncthreads();
+                    if (tid < 256) {
+                        uint32_t m = 0;
+                        for (int q = 0; q < p.passes; ++q)
+                            m |= uint32_t(p.gp_all[size_t(q) * 256 + tid] == n) << q;
+                        if (m) atomicOr(smask, m);
+                    }
+                    __syncthreads();
+                    uniform = *smask;
                 }
-                __syncthreads();
-                uniform = *smask;
                 if ((uniform >> pass) & 1u) return;  // every CTA of this pass leaves: a no-op pass
             }
-            const uint32_t all = (p.passes >= 32) ? 0xffffffffu : ((1u << p.passes) - 1u);
             const int before = __popc(~uniform & ((1u << pass) - 1u));  // executed passes before this one
             const int total = __popc(~uniform & all);
             if (p.copy_keys_in) {

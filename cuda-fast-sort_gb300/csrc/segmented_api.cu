@@ -94,8 +94,38 @@ __global__ void __launch_bounds__(256) seg_scan_kernel(SegScanParams p) {
     const uint32_t s = blockIdx.x / p.passes;
     const uint32_t pp = blockIdx.x % p.passes;
     const uint32_t c = p.seg_counts[(size_t(s) * p.passes + pp) * 256 + threadIdx.x];
-    const uint32_t excl = block_exclusive_scan_256<uint32_t>(c, tmp, nullptr);
+    uint32_t seg_len = 0;
+    const uint32_t excl = block_exclusive_scan_256<uint32_t>(c, tmp, &seg_len);
     p.seg_gofs[(size_t(pp) * p.segments + s) * 256 + threadIdx.x] = uint32_t(p.seg_begin[s]) + excl;
+    // the pass must run unless one digit holds this segment (for every segment)
+    if (!__syncthreads_or(c == seg_len) && threadIdx.x == 0) atomicOr(p.nonuniform, 1u << pp);
+}
+
+// Copies elements [0, bytes) of one range with the CTA's threads (words when
+// both ends allow).
+__device__ void cta_copy_bytes(uint8_t* dst, const uint8_t* src, uint64_t bytes) {
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 3u) == 0) {
+        const uint64_t w = bytes / 4;
+        for (uint64_t i = threadIdx.x; i < w; i += blockDim.x)
+            reinterpret_cast<uint32_t*>(dst)[i] = reinterpret_cast<const uint32_t*>(src)[i];
+        for (uint64_t i = w * 4 + threadIdx.x; i < bytes; i += blockDim.x) dst[i] = src[i];
+    } else {
+        for (uint64_t i = threadIdx.x; i < bytes; i += blockDim.x) dst[i] = src[i];
+    }
+}
+
+__global__ void __launch_bounds__(256) seg_fixup_kernel(SegFixupParams f) {
+    const uint32_t all = (1u << f.passes) - 1u;
+    if ((__popc(*f.nonuniform & all) & 1) == 0) return;  // an even number of passes ran: home already
+    for (uint32_t t = blockIdx.x; t < f.num_tiles; t += gridDim.x) {
+        const TileRec r = f.tiles[t];
+        cta_copy_bytes(static_cast<uint8_t*>(f.keys_a) + r.base * f.key_bytes,
+                       static_cast<const uint8_t*>(f.keys_b) + r.base * f.key_bytes, uint64_t(r.cnt) * f.key_bytes);
+        if (f.val_bytes)
+            cta_copy_bytes(static_cast<uint8_t*>(f.vals_a) + r.base * f.val_bytes,
+                           static_cast<const uint8_t*>(f.vals_b) + r.base * f.val_bytes,
+                           uint64_t(r.cnt) * f.val_bytes);
+    }
 }
 
 }  // namespace
@@ -258,6 +288,7 @@ int enqueue_segmented(SegPlan* p, cudaStream_t s) {
     }
     const size_t L = p->large_begin.size();
     const bool odd = (p->passes & 1) != 0;
+    const bool skip = gbsort_get_pass_skip() != 0;
     void* alt_keys = ws + p->alt_keys_off;
     void* alt_vals = p->vb ? ws + p->alt_vals_off : nullptr;
     int st;
@@ -284,6 +315,7 @@ int enqueue_segmented(SegPlan* p, cudaStream_t s) {
         sc.seg_gofs = reinterpret_cast<uint32_t*>(ws + p->seg_gofs_off);
         sc.segments = uint32_t(L);
         sc.passes = uint32_t(p->passes);
+        sc.nonuniform = ctl + 21;
         void* args[] = {&sc};
         e = cudaLaunchKernel(reinterpret_cast<const void*>(&seg_scan_kernel), dim3(uint32_t(L) * p->passes),
                              dim3(256), args, 0, s);
@@ -333,7 +365,36 @@ int enqueue_segmented(SegPlan* p, cudaStream_t s) {
             pp.wait_limit_ns = wait_limit_ns();
             pp.tiles = reinterpret_cast<const TileRec*>(ws + p->tiles_off);
             pp.seg_gofs = reinterpret_cast<const uint32_t*>(ws + p->seg_gofs_off) + size_t(pass) * L * 256;
+            pp.skip = skip ? 1 : 0;
+            pp.passes = p->passes;
+            pp.start_alt = odd ? 1 : 0;
+            pp.nonuniform_mask = ctl + 21;
+            pp.keys_a = p->keys;
+            pp.vals_a = p->vals;
+            pp.keys_b = alt_keys;
+            pp.vals_b = alt_vals;
             if ((st = launch(p->pass, grid, &pp, s, "segmented pass"))) return st;
+        }
+        if (skip && !odd) {  // odd pass counts start mirrored and always end at home
+            SegFixupParams fp{};
+            fp.tiles = reinterpret_cast<const TileRec*>(ws + p->tiles_off);
+            fp.num_tiles = T;
+            fp.passes = p->passes;
+            fp.nonuniform = ctl + 21;
+            fp.key_bytes = uint32_t(p->kb);
+            fp.val_bytes = uint32_t(p->vb);
+            fp.keys_b = alt_keys;
+            fp.keys_a = p->keys;
+            fp.vals_b = alt_vals;
+            fp.vals_a = p->vals;
+            void* args[] = {&fp};
+            e = cudaLaunchKernel(reinterpret_cast<const void*>(&seg_fixup_kernel),
+                                 dim3(std::max<uint32_t>(1, std::min<uint32_t>(T, uint32_t(device_sm_count()) * 4))),
+                                 dim3(256), args, 0, s);
+            if (e != cudaSuccess) {
+                set_last_error("segmented fixup", e);
+                return GBSORT_ERR_CUDA;
+            }
         }
     }
     return GBSORT_OK;
@@ -403,8 +464,10 @@ int gbsort_segmented_plan_info(const gbsort_segmented_plan* p, gbsort_segmented_
     out->cta_large_max = uint32_t(p->cta_l.tile);
     out->onesweep_tile = uint32_t(p->pass.tile);
     out->workspace_bytes = p->total_bytes;
-    out->kernel_launches = (p->large_begin.empty() ? 0 : 2 + uint64_t(p->passes)) + !p->small_l.empty() +
-                           !p->small_s.empty() + !p->small_s4.empty();
+    out->kernel_launches = (p->large_begin.empty()
+                                ? 0
+                                : 2 + uint64_t(p->passes) + ((gbsort_get_pass_skip() && (p->passes & 1) == 0) ? 1 : 0)) +
+                           !p->small_l.empty() + !p->small_s.empty() + !p->small_s4.empty();
     return GBSORT_OK;
 }
 

@@ -69,6 +69,8 @@ struct PassParams {
     // buffers so that the last one lands in the output.  nullptr: in place.
     const void* copy_keys_in;
     const void* copy_vals_in;
+    // batched mode: bit q set when pass q's digit varies inside some segment
+    const uint32_t* nonuniform_mask;
 };
 
 // The copy home after uniform-pass skipping left an odd number of executed
@@ -119,6 +121,21 @@ struct SegScanParams {
     uint32_t* seg_gofs;                   // [passes][segments][256]
     uint32_t segments;
     uint32_t passes;
+    uint32_t* nonuniform;                 // bit q: pass q's digit varies inside some segment
+};
+
+// Batched pass skipping: copies the onesweep segments' tiles home when an
+// odd number of passes ran.
+struct SegFixupParams {
+    const TileRec* tiles;
+    uint32_t num_tiles;
+    int passes;
+    const uint32_t* nonuniform;
+    uint32_t key_bytes, val_bytes;
+    const void* keys_b;
+    void* keys_a;
+    const void* vals_b;
+    void* vals_a;
 };
 
 // Small segments sorted whole inside one CTA's shared memory.

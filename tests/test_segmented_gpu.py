@@ -155,11 +155,15 @@ def test_autotuner_installs_paths_and_stays_exact(gb, cuda, oracle):
         gb.set_segmented_path("u32", 4, -1, -1)
 
 
+@pytest.mark.parametrize("skip", [True, False])
 @pytest.mark.parametrize("path", ["PATH_CTA_S", "PATH_CTA_S4", "PATH_CTA_L", "PATH_ONESWEEP"])
 @pytest.mark.parametrize("kt,mask", [("u32", 0x00000FFF), ("u64", 0x0000FF00FF0000FF), ("i16", 0x00FF)])
-def test_uniform_digits_per_segment(gb, cuda, oracle, path, kt, mask):
+def test_uniform_digits_per_segment(gb, cuda, oracle, path, kt, mask, skip):
     """Keys whose masked-out bytes are constant: those digit passes are
-    uniform inside every segment (the CTA sort short-circuits them)."""
+    uniform inside every segment.  The CTA sort short-circuits them; the
+    onesweep path skips them (u32: 2 of 4 run; u64: 3 of 8 run, ending with
+    the copy home; i16: 1 of 2 runs, copy home), or runs them all with
+    skipping off."""
     rng = np.random.default_rng(31)
     off = _layout(rng, 150, 2, 12, extras=(0, 1, 4095, 4096))
     n = int(off[-1])
@@ -169,9 +173,11 @@ def test_uniform_digits_per_segment(gb, cuda, oracle, path, kt, mask):
     vals = np.arange(n, dtype=np.uint32)
     vb = 4
     try:
+        gb.set_pass_skip(skip)
         gb.set_segmented_path(kt, vb, -1, getattr(gb, path))
         (r, v0, k, v), = _run(gb, cuda, kt, raw, vals, off, False)[0]
     finally:
         gb.set_segmented_path(kt, vb, -1, -1)
+        gb.set_pass_skip(True)
     ek, ev = _expected(oracle, kt, raw, vals, off, False)
     assert _eq(k, ek) and _eq(v, ev)
