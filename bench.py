@@ -68,6 +68,14 @@ CONFIGS = {
                         "64 GiB device pool"),
 }
 KEY_BYTES = {"u32": 4, "f32": 4, "u64": 8, "u128": 16}
+# The reference's own published throughput for the same workload (rsort on an
+# RTX 3080 Ti, data/logs/benchmark_data.py of the reference, ms -> Gkeys/s).
+PUBLISHED = {
+    "c2b": (22.4, "rsort, u32 keys 2^28, RTX 3080 Ti (benchmark_data.py:42: 11.972 ms)"),
+    "c1": (14.4, "rsort, u32 keys 2^20, RTX 3080 Ti (benchmark_data.py:34: 0.073 ms)"),
+    "c3a": (3.03, "rsort, u64 keys + u64 values 2^27, RTX 3080 Ti (benchmark_data.py:196: 44.281 ms)"),
+    "c3b": (1.53, "rsort, u128 keys 2^26, RTX 3080 Ti (benchmark_data.py:118: 43.993 ms)"),
+}
 PLAIN_METRIC = "sort throughput (Gkeys/s) and HBM roofline fraction"
 BATCHED_METRIC = "batched segmented sort throughput (Gkeys/s)"
 SERVING_METRIC = "serving throughput (Gkeys/s) under continuous batching, p50/p99 latency at load"
@@ -484,7 +492,10 @@ def bench_gbsort(args, cfg, world, rank, local):
         "metric": PLAIN_METRIC, "value": round(value, 3),
         "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": kt, "data": "synthetic",
+        "vs_baseline": (round(value / PUBLISHED[args.config][0], 3)
+                        if args.config in PUBLISHED and cfg["n"] == CONFIGS[args.config]["n"] else None),
+        "baseline_published": PUBLISHED.get(args.config, (None, None))[1],
+        "dtype": kt, "data": "synthetic",
         "config": {"workload": cfg["workload"], "n": n, "key": kt, "value_bytes": vb, "descending": desc,
                    "passes": passes, "radix_bits": 8, "tile_items": plan.tile_items,
                    "threads": plan.threads, "items_per_thread": plan.items_per_thread,
