@@ -13,7 +13,8 @@ template <int KB, int VB, class W, bool SEG, class S = PassShape<KB, VB>>
 KernelEntry make_pass_entry() {
     using G = PassGeom<KB, VB, S::THREADS, S::IPT>;
     return KernelEntry{
-        reinterpret_cast<const void*>(&onesweep_pass_kernel<KB, VB, W, S::THREADS, S::IPT, SEG, S::MIN_CTAS>),
+        reinterpret_cast<const void*>(
+            &onesweep_pass_kernel<KB, VB, W, S::THREADS, S::IPT, SEG, S::MIN_CTAS, S::LOOKBACK_WINDOW>),
         S::THREADS, S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
 }
 

@@ -195,7 +195,7 @@ struct PassGeom {
 // count), each segment's first tile publishes an inclusive prefix of its own
 // so lookback chains never cross segments, and digit bases come per segment
 // from p.seg_gofs.
-template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int MIN_CTAS>
+template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int MIN_CTAS, int LBW>
 __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassParams p) {
     using U = typename KeyBits<KB>::U;
     using V = typename ValBits<VB>::V;
@@ -492,7 +492,6 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
 
         // ---- per-bin tile totals, warp bases, early PARTIAL publication
         uint32_t total = 0, valid_total = 0;
-        constexpr int LBW = PassShape<KB, VB>::LOOKBACK_WINDOW;
         W lb_pre[LBW];
         if (tid < 256) {
 #pragma unroll

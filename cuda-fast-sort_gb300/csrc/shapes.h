@@ -53,12 +53,19 @@ constexpr ShapeRow pass_shape_small_row(int kb, int vb) {
 }
 constexpr uint64_t SMALL_N_MAX = uint64_t(1) << 22;
 
+// Predecessor tiles per lookback round trip for short arrays: all their tiles
+// are in flight at once, so the known-prefix frontier moves a window per L2
+// round trip (2^20 u32: 4 -> 8 took 14.0 -> 14.35 Gkeys/s; 16 and 32 slower).
+#ifndef GBSORT_SMALL_WINDOW
+#define GBSORT_SMALL_WINDOW 8
+#endif
+
 template <int KB, int VB>
 struct PassShapeSmall {
     static constexpr int THREADS = pass_shape_small_row(KB, VB).threads;
     static constexpr int IPT = pass_shape_small_row(KB, VB).ipt;
     static constexpr int MIN_CTAS = pass_shape_small_row(KB, VB).min_ctas;
-    static constexpr int LOOKBACK_WINDOW = 4;
+    static constexpr int LOOKBACK_WINDOW = GBSORT_SMALL_WINDOW;
 };
 
 template <int KB, int VB>
