@@ -325,7 +325,10 @@ def bench_gbsort(args, cfg, world, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream()
+    # a stream of its own (not the legacy default stream): input generation,
+    # flush, sorts and events are all ordered on it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     kt, n, vb, desc = cfg["key"], cfg["n"], cfg["vb"], cfg["desc"]
     kbytes = KEY_BYTES[kt]
     passes = kbytes

@@ -279,6 +279,9 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
             }
             twiddle_load = before == 0;
             twiddle_store = before + 1 == total;
+            if constexpr (!SEG) {
+                if (p.executed && blockIdx.x == 0 && tid == 0) *p.executed = 0x80000000u | uint32_t(total);
+            }
         }
     }
     const U* gkeys_in = static_cast<const U*>(keys_in);

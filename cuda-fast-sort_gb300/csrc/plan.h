@@ -14,18 +14,22 @@ namespace gbsort {
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Control block at the start of the workspace's control region:
-//   [gp_counts: passes*256 u64][tile_counters: 16 u32][err: u32][pad]
+//   [gp_counts: passes*256 u64][tile_counters: 16 u32][err: u32][executed: u32][pad]
+// executed: written by the pass kernels that run (bit 31 | passes executed)
+// when uniform passes are skipped; 0 when none ran.
 struct CtlLayout {
     size_t gp_off = 0;
     size_t counters_off = 0;
     size_t err_off = 0;
+    size_t exec_off = 0;
     size_t bytes = 0;
     static CtlLayout make(int passes) {
         CtlLayout c;
         c.gp_off = 0;
         c.counters_off = size_t(passes) * 256 * 8;
         c.err_off = c.counters_off + 16 * 4;
-        c.bytes = align_up(c.err_off + 4, 256);
+        c.exec_off = c.err_off + 4;
+        c.bytes = align_up(c.exec_off + 4, 256);
         return c;
     }
 };

@@ -71,13 +71,14 @@ struct PassParams {
     const void* copy_vals_in;
     // batched mode: bit q set when pass q's digit varies inside some segment
     const uint32_t* nonuniform_mask;
+    // plain mode with skipping: receives bit 31 | number of executed passes
+    uint32_t* executed;
 };
 
 // The copy home after uniform-pass skipping left an odd number of executed
 // passes (the result then sits in the alternate buffer).
 struct FixupParams {
-    const unsigned long long* gp_all;  // [passes][256]
-    uint64_t n;
+    const uint32_t* executed;  // bit 31 | executed passes, 0 when none ran
     int passes;
     const void* keys_b;
     void* keys_a;

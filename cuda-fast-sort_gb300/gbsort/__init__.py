@@ -608,3 +608,23 @@ def check_pairs(keys_in, keys_out, index_values, value_bytes: int, n: int, key_t
     _check(f(key_type_id(key_type), _ptr(keys_in), _ptr(keys_out), _ptr(index_values), value_bytes, n,
              _stream(stream), ctypes.byref(out)), "pairs")
     return out.value
+
+
+def set_graph_cache(enable: bool) -> None:
+    """Graph replay of repeated identical calls on/off (default on)."""
+    f = lib().gbsort_set_graph_cache
+    f.restype = None
+    f.argtypes = [ctypes.c_int]
+    f(int(enable))
+
+
+def get_graph_cache() -> bool:
+    f = lib().gbsort_get_graph_cache
+    f.restype = ctypes.c_int
+    return bool(f())
+
+
+def graph_cache_clear() -> None:
+    f = lib().gbsort_graph_cache_clear
+    f.restype = ctypes.c_int
+    _check(f(), "graph cache clear")

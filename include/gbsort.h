@@ -389,6 +389,19 @@ int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n,
 void gbsort_set_pass_skip(int enable);
 int gbsort_get_pass_skip(void);
 
+/* Graph replay of repeated calls (default on; GBSORT_GRAPH_CACHE=0 turns it
+ * off at load).  The second call of gbsort_sort_keys / _pairs / _copy with
+ * the same buffers, size, key type, order, stream and settings is captured
+ * into a CUDA graph, and later identical calls replay it, which removes the
+ * gaps between the sort's kernels (what the reference does on every call,
+ * include/rsort/detail/radix_kernel.cuh:583-601, without its per-call
+ * capture cost).  Nothing is captured on the legacy stream or on a stream
+ * the caller is capturing; up to 32 graphs are kept per process.
+ * gbsort_graph_cache_clear synchronizes the device and frees them. */
+void gbsort_set_graph_cache(int enable);
+int gbsort_get_graph_cache(void);
+int gbsort_graph_cache_clear(void);
+
 /* Upper bound, in nanoseconds, on any single device-side wait (lookback spin
  * or TMA barrier) of later launches.  Default 2e9 (2 s).  Process-wide. */
 void gbsort_set_wait_limit_ns(uint64_t ns);
