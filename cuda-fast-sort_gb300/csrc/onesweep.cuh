@@ -363,8 +363,10 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
     // Tile ids come from the pass's atomic counter.  Thread 0 claims the next
     // tile when the current one starts and bulk-copies it into the other
     // buffer meanwhile (GBSORT_TILE_LOOKAHEAD 3 claims two more ahead).
+#if GBSORT_TILE_LOOKAHEAD >= 3
     uint32_t id_an = 0, id_aan = 0;  // thread 0: ids of the tiles after next
     TileRec rec_an{};                // thread 0: table entry of id_an
+#endif
     __syncthreads();
     if (tid == 0) {
         const uint32_t t0 = atomicAdd(p.tile_counter, 1u);
