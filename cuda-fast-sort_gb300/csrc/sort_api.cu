@@ -519,10 +519,15 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
             return direct();
         }
     }
-    const cudaError_t err = cudaGraphLaunch(e->exec, s);
-    if (err != cudaSuccess) {
-        set_last_error("graph launch", err);
-        return GBSORT_ERR_CUDA;
+    if (cudaGraphLaunch(e->exec, s) != cudaSuccess) {
+        // a graph that no longer launches (e.g. its context was reset) is
+        // dropped; the call goes direct and reports what the direct path sees
+        cudaGetLastError();
+        cudaGraphExecDestroy(e->exec);
+        cudaGetLastError();
+        *e = g_graphs.back();
+        g_graphs.pop_back();
+        return direct();
     }
     return GBSORT_OK;
 }
