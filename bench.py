@@ -1,19 +1,27 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 onesweep LSD radix sort (libgbsort.so, C ABI).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2b|c1|c2a|c3a|c3b]
-                    [--impl gbsort|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W]
+                    [--config c2b|c1|c2a|c3a|c3b|c4|c5] [--impl gbsort|reference]
+                    [--n N] [--rate R] [--e2e-steps S] [--cpu-seconds T]
+                    [--no-cpu-baseline] [--no-cub]
 
 One step = one sort (histogram upsweep + one onesweep pass per key byte) of a
 fresh batch of synthetic keys already resident in HBM.  Before each step the
 next batch is generated on the device (splitmix64 stream, new seed) and a
-512 MiB buffer is written to flush L2; CUDA events on the sort's stream time
-the sort alone, and `value` = keys sorted / summed event time.  The K timed
-steps are bracketed by a barrier + torch.cuda.synchronize() on both sides.
+512 MiB buffer is written to flush L2; CUDA events on the sort's stream (a
+stream of its own) time the sort alone, and `value` = keys sorted / summed
+event time.  The K timed steps are bracketed by a barrier +
+torch.cuda.synchronize() on both sides.
 
 Default workload (the headline): 2^28 uint32 keys, uniform full range,
-ascending, keys only, 8-bit digits / 4 passes.  Other --config values are the
-other configurations of the reference's benchmark table.
+ascending, keys only, 8-bit digits / 4 passes.  c1, c2a, c3a, c3b are the
+reference benchmark's other plain configurations; c4 is the batched sort of
+4096 uneven segments (step = one replay of the batched run, compared with
+looping the plain sort over the same segments); c5 is the sort server under
+Poisson arrivals from host memory (capacity, then p50/p99 latency at a
+fraction of it).  --n shrinks a plain configuration for profiling; --rate
+sets c5's arrival rate.
 
 Extra keys on the JSON line:
   roofline      the dominant kernel (the onesweep pass): algorithmic bytes per
