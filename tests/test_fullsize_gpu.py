@@ -85,3 +85,59 @@ def test_u128_keys_2p26_desc(gb, cuda):
     expect = keys[perm]
     _sort(gb, torch, "u128", keys, n, desc=True)
     assert torch.equal(keys, expect)
+
+
+@pytest.mark.parametrize("kt,kb,n,vb", [
+    ("u16", 2, (1 << 29) + 12345, 0),   # 2 passes: 64-bit status words past 2^29
+    ("i32", 4, (1 << 28) + 4097, 4),    # 4 passes: past 2^28, with index values
+    ("f64", 8, (1 << 27) + 777, 8),     # 8 passes: past 2^27, with index values
+    ("u128", 16, (1 << 26) + 5, 0),     # 16 passes: past 2^26
+])
+def test_wide_status_words(gb, cuda, kt, kb, n, vb):
+    """Sizes just past each key width's 32-bit status-word limit
+    (n > 2^(30 - log2 passes)) run the 64-bit status instantiations; checked
+    on the device: sorted order, the same multiset of keys, and (with index
+    values) every value pointing at an input key equal to its output key."""
+    torch = cuda
+    plan = gb.plan(kt, n, vb)
+    assert plan.status_word_bytes == 8
+    keys = torch.empty(n * kb, dtype=torch.uint8, device="cuda")
+    gb.generate(4, kb, keys, n, 99)  # the reference's random mode (duplicates for u16)
+    src = keys.clone()
+    vals = None
+    if vb:
+        vals = torch.empty(n * vb, dtype=torch.uint8, device="cuda")
+        gb.generate(3, vb, vals, n, 0)  # original index
+    for desc in (False, True):
+        keys.copy_(src)
+        if vb:
+            gb.generate(3, vb, vals, n, 0)
+        _sort(gb, torch, kt, keys, n, vals, vb, desc)
+        assert gb.check_order(keys, n, kt, desc) == 0
+        assert gb.checksum(keys, n, kt) == gb.checksum(src, n, kt)
+        if vb:
+            assert gb.check_pairs(src, keys, vals, vb, n, kt) == 0
+
+
+@pytest.mark.parametrize("kt,vb", [("u32", 0), ("f32", 4), ("u64", 8)])
+def test_short_array_shape_boundary(gb, cuda, oracle, kt, vb):
+    """n <= 2^22 takes the short-array pass shape, larger n the default one:
+    both sides of the switch against the oracle."""
+    import os
+
+    import numpy as np
+
+    from _oracle import raw_keys, raw_values
+    from gpu_util import gpu_sort
+
+    threads = max(1, min(16, os.cpu_count() or 1))
+    for n in ((1 << 22) - 1, 1 << 22, (1 << 22) + 1):
+        raw = raw_keys(kt, n, seed=n, dist=4)
+        vals = raw_values(vb, n, seed=1)
+        got = gpu_sort(gb, cuda, kt, raw, False, vals)
+        ref = oracle.sort(kt, raw, False, vals, threads=threads)
+        if vals is None:
+            assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), n
+        else:
+            assert np.array_equal(got[0].view(np.uint8), ref[0].view(np.uint8)), n
+            assert np.array_equal(got[1].view(np.uint8), ref[1].view(np.uint8)), n
