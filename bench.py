@@ -125,6 +125,32 @@ def committed_traffic(config: str, n: int):
         return None, None
 
 
+class TimedRange:
+    """An NVTX push/pop range named "timed" around a timed region, so that a
+    launch list can be restricted to it (ncu --nvtx --nvtx-include "timed]").
+    Host-side only; a missing NVTX library leaves it a no-op."""
+
+    def __enter__(self):
+        try:
+            import torch
+
+            torch.cuda.nvtx.range_push("timed")
+            self.on = True
+        except Exception:
+            self.on = False
+        return self
+
+    def __exit__(self, *exc):
+        if self.on:
+            try:
+                import torch
+
+                torch.cuda.nvtx.range_pop()
+            except Exception:
+                pass
+        return False
+
+
 class ClockSampler:
     """nvidia-smi -lms 200 in the background while the timed region runs."""
 
@@ -586,7 +612,8 @@ def bench_batched(args, cfg, world, rank, local):
         prepare(100 + i)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        plan.run(stream=stream)
+        with TimedRange():
+            plan.run(stream=stream)
         b.record(stream)
         ev.append((a, b))
     torch.cuda.synchronize()

@@ -20,7 +20,7 @@
 
 namespace gbsort {
 
-constexpr int SEG_UP_THREADS = 512;
+constexpr int SEG_UP_THREADS = 1024;
 
 // CTA-wide copy of `bytes` bytes (16-byte vectors when both sides allow).
 __device__ __forceinline__ void block_copy(uint8_t* dst, const uint8_t* src, uint64_t bytes) {
@@ -34,12 +34,15 @@ __device__ __forceinline__ void block_copy(uint8_t* dst, const uint8_t* src, uin
     }
 }
 
+// Counters [bin][copy], copy = lane % COPIES.  With 32 copies (keys up to 4
+// bytes, 32-128 KB) every lane of a warp owns a bank and the atomics never
+// conflict; wider keys keep 32 KB with 4 or 2 copies.
 template <int KB>
 struct SegHistGeom {
     static constexpr int P = KB;
-    static constexpr int COPIES = P <= 4 ? 8 : (P == 8 ? 4 : 2);
+    static constexpr int COPIES = P <= 4 ? 32 : (P == 8 ? 4 : 2);
     static constexpr int NBINS = P * 256;
-    static constexpr size_t SMEM_BYTES = size_t(NBINS) * COPIES * 4;  // 32 KB
+    static constexpr size_t SMEM_BYTES = size_t(NBINS) * COPIES * 4;
 };
 
 template <int KB>
@@ -86,7 +89,22 @@ __global__ void __launch_bounds__(SEG_UP_THREADS) seg_upsweep_kernel(SegUpsweepP
         const uint64_t nvec = (m - head) / PER_VEC;
         if (uint64_t(tid) < head) count(k0[tid]);
         const uint4* vec = reinterpret_cast<const uint4*>(k0 + head);
-        for (uint64_t i = tid; i < nvec; i += SEG_UP_THREADS) {
+        // four 16-byte loads in flight per thread before their counts
+        constexpr int UNROLL = 4;
+        uint64_t i = tid;
+        for (; i + (UNROLL - 1) * SEG_UP_THREADS < nvec; i += UNROLL * SEG_UP_THREADS) {
+            uint4 v[UNROLL];
+#pragma unroll
+            for (int r = 0; r < UNROLL; ++r) v[r] = __ldcs(vec + i + r * SEG_UP_THREADS);
+#pragma unroll
+            for (int r = 0; r < UNROLL; ++r) {
+                union { uint4 q; U k[PER_VEC]; } u;
+                u.q = v[r];
+#pragma unroll
+                for (int e = 0; e < PER_VEC; ++e) count(u.k[e]);
+            }
+        }
+        for (; i < nvec; i += SEG_UP_THREADS) {
             union { uint4 q; U k[PER_VEC]; } u;
             u.q = __ldcs(vec + i);
 #pragma unroll

@@ -442,8 +442,10 @@ int check_args(int key_type, size_t value_bytes, void* d_keys, void* d_values, s
 // comes a second time, and replayed from then on; one-off calls launch
 // directly, and nothing is captured on the legacy stream or on a stream the
 // caller is capturing.  Graph launches cut the gaps between the sort's
-// kernels (2^20 u32 keys: 76 -> 63 us).  At most GRAPH_CAP graphs are kept;
-// gbsort_graph_cache_clear() frees them.
+// kernels (2^20 u32 keys: 76 -> 63 us).  The GRAPH_CAP most recently used
+// calls are tracked; a new call replaces the least recently used one (its
+// graph, if any, is destroyed; one still running is freed by CUDA when it
+// completes).  gbsort_graph_cache_clear() frees them all.
 struct GraphKey {
     int device, key_type, desc, skip;
     size_t vb;
@@ -456,10 +458,14 @@ struct GraphKey {
 struct GraphEntry {
     GraphKey key;
     cudaGraphExec_t exec = nullptr;
+    uint64_t last_use = 0;
 };
 constexpr size_t GRAPH_CAP = 32;
 std::mutex g_graph_mu;
 std::vector<GraphEntry> g_graphs;
+uint64_t g_graph_tick = 0;      // guarded by g_graph_mu
+uint64_t g_graph_replays = 0;   // graph launches, guarded by g_graph_mu
+uint64_t g_graph_captures = 0;  // graphs instantiated, guarded by g_graph_mu
 std::atomic<int> g_graph_cache{[] {
     const char* v = std::getenv("GBSORT_GRAPH_CACHE");
     return (v && v[0] == '0') ? 0 : 1;
@@ -494,9 +500,18 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
     for (auto& g : g_graphs)
         if (g.key == k) e = &g;
     if (e == nullptr) {  // first time: remember it, launch directly
-        if (g_graphs.size() < GRAPH_CAP) g_graphs.push_back(GraphEntry{k, nullptr});
+        if (g_graphs.size() < GRAPH_CAP) {
+            g_graphs.push_back(GraphEntry{k, nullptr, ++g_graph_tick});
+        } else {
+            GraphEntry* lru = &g_graphs[0];
+            for (auto& g : g_graphs)
+                if (g.last_use < lru->last_use) lru = &g;
+            if (lru->exec) cudaGraphExecDestroy(lru->exec);
+            *lru = GraphEntry{k, nullptr, ++g_graph_tick};
+        }
         return direct();
     }
+    e->last_use = ++g_graph_tick;
     if (e->exec == nullptr) {  // second time: capture (the kernels are prepared by now)
         cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) {
@@ -518,6 +533,7 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
             cudaGetLastError();
             return direct();
         }
+        ++g_graph_captures;
     }
     if (cudaGraphLaunch(e->exec, s) != cudaSuccess) {
         // a graph that no longer launches (e.g. its context was reset) is
@@ -529,6 +545,7 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
         g_graphs.pop_back();
         return direct();
     }
+    ++g_graph_replays;
     return GBSORT_OK;
 }
 
@@ -773,6 +790,16 @@ int gbsort_graph_cache_clear(void) {
         return GBSORT_ERR_CUDA;
     }
     return GBSORT_OK;
+}
+
+void gbsort_graph_cache_stats(uint64_t* calls, uint64_t* graphs, uint64_t* captures, uint64_t* replays) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    uint64_t with_graph = 0;
+    for (const auto& g : g_graphs) with_graph += g.exec != nullptr;
+    if (calls) *calls = g_graphs.size();
+    if (graphs) *graphs = with_graph;
+    if (captures) *captures = g_graph_captures;
+    if (replays) *replays = g_graph_replays;
 }
 
 void gbsort_set_pass_skip(int enable) { g_pass_skip.store(enable ? 1 : 0, std::memory_order_relaxed); }

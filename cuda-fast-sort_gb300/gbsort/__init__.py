@@ -628,3 +628,13 @@ def graph_cache_clear() -> None:
     f = lib().gbsort_graph_cache_clear
     f.restype = ctypes.c_int
     _check(f(), "graph cache clear")
+
+
+def graph_cache_stats() -> dict:
+    """Tracked calls, those holding a graph, graphs captured and replays since load."""
+    f = lib().gbsort_graph_cache_stats
+    f.restype = None
+    f.argtypes = [ctypes.POINTER(ctypes.c_uint64)] * 4
+    v = [ctypes.c_uint64(0) for _ in range(4)]
+    f(*[ctypes.byref(x) for x in v])
+    return dict(zip(("calls", "graphs", "captures", "replays"), (x.value for x in v)))

@@ -396,11 +396,16 @@ int gbsort_get_pass_skip(void);
  * gaps between the sort's kernels (what the reference does on every call,
  * include/rsort/detail/radix_kernel.cuh:583-601, without its per-call
  * capture cost).  Nothing is captured on the legacy stream or on a stream
- * the caller is capturing; up to 32 graphs are kept per process.
- * gbsort_graph_cache_clear synchronizes the device and frees them. */
+ * the caller is capturing.  The 32 most recently used calls are tracked per
+ * process; a new one replaces the least recently used (and its graph).
+ * gbsort_graph_cache_clear synchronizes the device and frees them.
+ * gbsort_graph_cache_stats: tracked calls, of those the ones holding a graph,
+ * and graphs captured and replays launched since load (any pointer may be
+ * NULL). */
 void gbsort_set_graph_cache(int enable);
 int gbsort_get_graph_cache(void);
 int gbsort_graph_cache_clear(void);
+void gbsort_graph_cache_stats(uint64_t* calls, uint64_t* graphs, uint64_t* captures, uint64_t* replays);
 
 /* Upper bound, in nanoseconds, on any single device-side wait (lookback spin
  * or TMA barrier) of later launches.  Default 2e9 (2 s).  Process-wide. */

@@ -90,3 +90,32 @@ def test_inside_callers_capture(gb, cuda, oracle):
         cuda.cuda.synchronize()
         raw = src.cpu().numpy().view(np.uint32)
         assert _eq(dk.cpu().numpy().view(np.uint32), oracle.sort("u32", raw))
+
+
+def test_least_recently_used_call_is_replaced(gb, cuda):
+    """Once 32 calls are tracked, a new call replaces the least recently used
+    one, so a call repeated after many distinct ones still gets its graph."""
+    s = cuda.cuda.Stream()
+    nmax = 8000
+    dk = cuda.empty(nmax * 4, dtype=cuda.uint8, device="cuda")
+    tb = gb.temp_bytes("u32", nmax)
+    ws = cuda.empty(tb, dtype=cuda.uint8, device="cuda")
+    gb.generate(0, 4, dk, nmax, 9)
+    cuda.cuda.synchronize()
+    gb.graph_cache_clear()
+    for i in range(40):  # 40 distinct calls, each once
+        gb.sort(dk, 1000 + i, "u32", ws, tb, stream=s)
+    s.synchronize()
+    st0 = gb.graph_cache_stats()
+    assert st0["calls"] == 32 and st0["graphs"] == 0
+    for rep in range(3):  # tracked, captured + launched, replayed
+        gb.generate(0, 4, dk, nmax, 20 + rep)
+        cuda.cuda.synchronize()
+        gb.sort(dk, 5000, "u32", ws, tb, stream=s)
+        s.synchronize()
+        assert gb.check_order(dk, 5000, "u32") == 0, rep
+    st1 = gb.graph_cache_stats()
+    assert st1["calls"] == 32 and st1["graphs"] == 1
+    assert st1["captures"] == st0["captures"] + 1 and st1["replays"] == st0["replays"] + 2
+    gb.graph_cache_clear()
+    assert gb.graph_cache_stats()["calls"] == 0
