@@ -509,10 +509,19 @@ def bench_gbsort(args, cfg, world, rank, local):
                              stream=stream)
             e2e_t.append(time.perf_counter() - t0)
         e2e_t = e2e_t[1:]  # first call is a warm-up
+        # the last result, back on the device: in order, and a permutation of the input
+        chk = dbuf[:hbytes]
+        chk.copy_(h_work)
+        torch.cuda.synchronize()
+        ordered = gbsort.check_order(chk, n, kt, descending=desc) == 0
+        sum_out = gbsort.checksum(chk, n, kt)
+        chk.copy_(h_src)
+        torch.cuda.synchronize()
+        e2e_ok = ordered and sum_out == gbsort.checksum(chk, n, kt)
         e2e = {"value": round(n / statistics.mean(e2e_t) / 1e9, 4), "unit": "Gkeys/s",
                "h2d_bytes_per_step": n * (kbytes + vb), "d2h_bytes_per_step": n * (kbytes + vb),
                "steps": e2e_steps, "ms_per_step": round(1000 * statistics.mean(e2e_t), 3),
-               "api": "gbsort_sort_host (pinned host buffers)"}
+               "api": "gbsort_sort_host (pinned host buffers)", "checked": e2e_ok}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -73,6 +73,7 @@ int resident_ctas(const KernelEntry& e);  // per SM, after opting in to the smem
 int prepare_kernel(const KernelEntry& e); // cudaFuncSetAttribute once per device
 
 uint64_t wait_limit_ns();
+int status_from_error_word(uint32_t err);  // workspace error word -> gbsort_status
 void set_last_error(const char* what, cudaError_t err);
 void set_last_error_text(const char* text);
 

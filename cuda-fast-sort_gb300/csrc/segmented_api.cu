@@ -498,6 +498,10 @@ int segmented_bind_image(gbsort_segmented_plan* p, void* d_keys, void* d_values,
                          size_t workspace_bytes, void* stream, const uint8_t* image) {
     if (!p || (p->num_segments && !d_keys) || (p->vb && p->num_segments && !d_values)) return GBSORT_ERR_INVALID_ARGUMENT;
     if (d_workspace == nullptr || workspace_bytes < p->total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    if (reinterpret_cast<uintptr_t>(d_workspace) % 16) {  // the status array is cleared by 16-byte stores
+        set_last_error_text("the workspace must be 16-byte aligned");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
     if ((reinterpret_cast<uintptr_t>(d_keys) % p->kb) || (p->vb && reinterpret_cast<uintptr_t>(d_values) % p->vb))
         return GBSORT_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(p->mu);

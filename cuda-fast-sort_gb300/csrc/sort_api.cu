@@ -268,6 +268,10 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
                  const void* vals_src) {
     if (n_ms) *n_ms = 0;
     if (plan.n == 0) return GBSORT_OK;
+    if (reinterpret_cast<uintptr_t>(d_workspace) % 16) {  // the status array is cleared by 16-byte stores
+        set_last_error_text("the workspace must be 16-byte aligned");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
     if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
     int st = prepare_kernel(plan.pass);
     if (st != GBSORT_OK) return st;
@@ -410,6 +414,12 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     return GBSORT_OK;
 }
 
+int status_from_error_word(uint32_t err) {
+    if (err & ERRBIT_BOUNDS) return GBSORT_ERR_INTERNAL;
+    if (err & ERRBIT_TIMEOUT) return GBSORT_ERR_TIMEOUT;
+    return GBSORT_OK;
+}
+
 }  // namespace gbsort
 
 using namespace gbsort;
@@ -418,12 +428,6 @@ namespace {
 
 bool naturally_aligned(const void* p, size_t bytes) {
     return p == nullptr || bytes == 0 || (reinterpret_cast<uintptr_t>(p) % bytes) == 0;
-}
-
-int status_from_error_word(uint32_t err) {
-    if (err & ERRBIT_BOUNDS) return GBSORT_ERR_INTERNAL;
-    if (err & ERRBIT_TIMEOUT) return GBSORT_ERR_TIMEOUT;
-    return GBSORT_OK;
 }
 
 int check_args(int key_type, size_t value_bytes, void* d_keys, void* d_values, size_t* temp_bytes) {
@@ -693,52 +697,6 @@ GBSORT_DEFINE_TYPED(f32, GBSORT_KEY_F32)
 GBSORT_DEFINE_TYPED(f64, GBSORT_KEY_F64)
 GBSORT_DEFINE_TYPED(f128, GBSORT_KEY_F128)
 #undef GBSORT_DEFINE_TYPED
-
-size_t gbsort_host_buffer_bytes(int key_type, size_t value_bytes, size_t n) {
-    Plan plan;
-    if (make_plan(key_type, value_bytes, n, &plan) != GBSORT_OK) return 0;
-    size_t off = align_up(n * size_t(plan.kb), 256);
-    off = align_up(off + n * value_bytes, 256);
-    return off + plan.total_bytes;
-}
-
-int gbsort_sort_host(int key_type, int descending, void* h_keys, void* h_values, size_t value_bytes, size_t n,
-                     void* d_buffer, size_t buffer_bytes, void* stream) {
-    Plan plan;
-    int st = make_plan(key_type, value_bytes, n, &plan);
-    if (st != GBSORT_OK) return st;
-    if (n == 0) return GBSORT_OK;
-    if (h_keys == nullptr || d_buffer == nullptr || (value_bytes && h_values == nullptr))
-        return GBSORT_ERR_INVALID_ARGUMENT;
-    const size_t need = gbsort_host_buffer_bytes(key_type, value_bytes, n);
-    if (buffer_bytes < need) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    uint8_t* base = static_cast<uint8_t*>(d_buffer);
-    const size_t kbytes = n * size_t(plan.kb), vbytes = n * value_bytes;
-    uint8_t* d_keys = base;
-    uint8_t* d_vals = base + align_up(kbytes, 256);
-    uint8_t* d_ws = base + align_up(align_up(kbytes, 256) + vbytes, 256);
-    cudaError_t e = cudaMemcpyAsync(d_keys, h_keys, kbytes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && vbytes) e = cudaMemcpyAsync(d_vals, h_values, vbytes, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) {
-        set_last_error("host to device copy", e);
-        return GBSORT_ERR_CUDA;
-    }
-    st = enqueue_sort(plan, descending ? 1 : 0, d_keys, value_bytes ? d_vals : nullptr, d_ws, s, nullptr, 0,
-                      nullptr);
-    if (st != GBSORT_OK) return st;
-    e = cudaMemcpyAsync(h_keys, d_keys, kbytes, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && vbytes) e = cudaMemcpyAsync(h_values, d_vals, vbytes, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        set_last_error("device to host copy", e);
-        return GBSORT_ERR_CUDA;
-    }
-    uint32_t err = 0;
-    e = cudaMemcpy(&err, d_ws + plan.ctl_off + plan.ctl.err_off, 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return GBSORT_ERR_CUDA;
-    return status_from_error_word(err);
-}
 
 int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {
     Plan plan;

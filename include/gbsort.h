@@ -18,7 +18,9 @@
  * Protocol (same as rsort): call once with workspace == NULL to learn
  * *temp_bytes, allocate that many device bytes, call again with the
  * workspace; keys (and values) are sorted in place, ping-ponging through the
- * workspace.  The library allocates no device memory on this path.
+ * workspace.  The library allocates no device memory on this path.  The
+ * workspace must be 16-byte aligned (cudaMalloc returns 256-byte aligned
+ * memory); an unaligned one is refused with GBSORT_ERR_INVALID_ARGUMENT.
  *
  * Deliberate differences from rsort, all in the caller's favour:
  *   - the stream argument is honoured (rsort replaces it by a private stream
@@ -163,10 +165,17 @@ int gbsort_sort_keys_noalloc(int key_type, int descending, void* d_keys,
                              size_t n, void* stream);
 
 /* Sort from HOST buffers: copies n keys (and values) from host memory into
- * the caller's device buffer d_buffer, sorts them there and copies the result
- * back, all on `stream`, then synchronizes the stream.  d_buffer must hold
- * gbsort_host_buffer_bytes(...) bytes (keys + values + workspace); pinned host
- * memory gives full copy bandwidth.  No allocation happens inside. */
+ * the caller's device buffer d_buffer (16-byte aligned), sorts them there and
+ * copies the result back, then synchronizes.  d_buffer must hold
+ * gbsort_host_buffer_bytes(...) bytes (twice the keys and values, plus
+ * control words); pinned host memory gives full copy bandwidth.  No
+ * allocation happens inside.  Arrays of >= GBSORT_HOST_SPLIT_MIN keys
+ * (environment, default 2^24; keys of 2 bytes or more) are partitioned by
+ * their top digit first and sorted in about GBSORT_HOST_SPLIT_GROUPS
+ * (default 16) groups of consecutive buckets, each copied back on a
+ * library-owned copy stream while the next ones sort; the work is ordered
+ * after what `stream` already holds.  Smaller arrays are copied in, sorted
+ * and copied back on `stream`.  Either way the result is the in-place sort's. */
 size_t gbsort_host_buffer_bytes(int key_type, size_t value_bytes, size_t n);
 int gbsort_sort_host(int key_type, int descending, void* h_keys,
                      void* h_values, size_t value_bytes, size_t n,
