@@ -107,12 +107,6 @@ cudaStream_t copy_stream() {
     return streams[dev];
 }
 
-uint32_t upsweep_ctas(uint64_t keys, int kb) {
-    const uint64_t work = (keys * uint64_t(kb) + HIST_THREADS * 64ull - 1) / (HIST_THREADS * 64ull);
-    const uint64_t sms = uint64_t(std::max(1, device_sm_count()));
-    return uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(work, sms)));
-}
-
 uint32_t pass_ctas(const Plan& p) {
     const uint64_t cap = uint64_t(std::max(1, device_sm_count())) * uint64_t(std::max(1, resident_ctas(p.pass)));
     return uint32_t(std::min<uint64_t>(p.num_tiles, cap));

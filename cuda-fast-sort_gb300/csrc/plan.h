@@ -71,6 +71,7 @@ int device_sm_count();
 int device_is_sm103();
 int resident_ctas(const KernelEntry& e);  // per SM, after opting in to the smem
 int prepare_kernel(const KernelEntry& e); // cudaFuncSetAttribute once per device
+uint32_t upsweep_ctas(uint64_t n, int kb);  // grid of the plain upsweep
 
 uint64_t wait_limit_ns();
 int status_from_error_word(uint32_t err);  // workspace error word -> gbsort_status

@@ -208,6 +208,16 @@ int device_is_sm103() {
     return f && f->cc == 103;
 }
 
+// Upsweep CTAs (one per SM at most): one per 64 KB of keys.  Short arrays
+// keep few CTAs: every CTA ends with one global atomic per digit bin, and at
+// 2^20 u32 keys 152 CTAs of 27 KB took 16.0 us against 12.2 us for 64 of
+// 64 KB.
+uint32_t upsweep_ctas(uint64_t n, int kb) {
+    const uint64_t work = (n * uint64_t(kb) + HIST_THREADS * 64ull - 1) / (HIST_THREADS * 64ull);
+    const uint64_t sms = uint64_t(device_sm_count() > 0 ? device_sm_count() : 1);
+    return uint32_t(work < 1 ? 1 : (work < sms ? work : sms));
+}
+
 int prepare_kernel(const KernelEntry& e) {
     KernelPrep* p = prep_for(e);
     return p ? p->status : GBSORT_ERR_CUDA;
@@ -324,10 +334,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     hp.vals = copy ? vals_src : d_values;
     hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
     hp.val_bytes_total = plan.n * uint64_t(plan.vb);
-    const uint64_t hist_work = (plan.n * uint64_t(plan.kb) + (HIST_THREADS * 64ull) - 1) /
-                               (HIST_THREADS * 64ull);
-    uint32_t hist_ctas = uint32_t(hist_work < uint64_t(sms) ? hist_work : uint64_t(sms));
-    if (hist_ctas == 0) hist_ctas = 1;
+    const uint32_t hist_ctas = upsweep_ctas(plan.n, plan.kb);
     {
         void* args[] = {&hp};
         if (timed) cudaEventRecord(ev[0], stream);
@@ -782,7 +789,7 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
     if (sms > 0 && prepare_kernel(plan.pass) == GBSORT_OK) {
         const uint64_t max_ctas = uint64_t(sms) * uint64_t(resident_ctas(plan.pass));
         out->pass_ctas = uint32_t(plan.num_tiles < max_ctas ? plan.num_tiles : max_ctas);
-        out->hist_ctas = uint32_t(sms);
+        out->hist_ctas = upsweep_ctas(plan.n, plan.kb);
     }
     out->status_word_bytes = plan.wide_status ? 8 : 4;
     out->kernel_launches = uint32_t(plan.passes + 1 + ((gbsort_get_pass_skip() && (plan.passes & 1) == 0) ? 1 : 0));
