@@ -30,8 +30,10 @@ Extra keys on the JSON line:
                 `traffic` = ncu dram bytes per launch from profiles/ when a
                 capture of this workload is committed there
   sort_roofline the whole sort: (K + P*2*(K+V)) bytes per key / sort time
+  step_ms       mean, std, p50, p99, min, max of the per-step CUDA-event times
   e2e           same metric through gbsort_sort_host with pinned HOST buffers,
-                H2D + sort + D2H inside the timed region
+                H2D + sort + D2H inside the timed region; `checked`: the
+                returned keys are in order and a permutation of the input
   cpu_baseline  the CPU oracle (std::stable_sort of twiddled keys, 1 thread)
                 on a bounded sample of the same workload (rank 0, N=1 only)
   clocks        nvidia-smi samples taken during the timed region
@@ -107,6 +109,15 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def step_stats(ms: list) -> dict:
+    """Mean, standard deviation and percentiles of per-step device times (ms)."""
+    v = sorted(ms)
+    pick = lambda q: v[min(len(v) - 1, int(round(q * (len(v) - 1))))]  # noqa: E731
+    return {"mean": round(statistics.mean(v), 4), "std": round(statistics.pstdev(v), 4),
+            "p50": round(pick(0.5), 4), "p99": round(pick(0.99), 4), "min": round(v[0], 4),
+            "max": round(v[-1], 4), "n": len(v)}
 
 
 def committed_traffic(config: str, n: int):
@@ -537,7 +548,8 @@ def bench_gbsort(args, cfg, world, rank, local):
     line = {
         "metric": PLAIN_METRIC, "value": round(value, 3),
         "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": round(total_ms / args.steps, 4), "step_ms": step_stats(sort_ms),
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": (round(value / PUBLISHED[args.config][0], 3)
                         if args.config in PUBLISHED and cfg["n"] == CONFIGS[args.config]["n"] else None),
         "baseline_published": PUBLISHED.get(args.config, (None, None))[1],
@@ -728,7 +740,8 @@ def bench_batched(args, cfg, world, rank, local):
     line = {
         "metric": BATCHED_METRIC, "value": round(value, 3), "unit": "Gkeys/s",
         "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": kt, "data": "synthetic",
+        "step_ms": step_stats(ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": kt,
+        "data": "synthetic",
         "config": {"workload": cfg["workload"], "n_keys": n, "segments": len(sizes), "value_bytes": vb,
                    "sharding": {"global_segments": len(sizes_all), "ranks": world,
                                 "rank_bytes": [int(x) for x in rank_bytes]} if world > 1 else None,
