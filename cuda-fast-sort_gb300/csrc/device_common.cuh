@@ -110,6 +110,16 @@ template <> struct ValBits<4> { using V = uint32_t; };
 template <> struct ValBits<8> { using V = uint64_t; };
 template <> struct ValBits<16> { using V = Val16; };
 
+// Programmatic dependent launch.  A kernel launched with the
+// programmatic-stream-serialization attribute may be scheduled while its
+// predecessor in the stream is still running: grid_dependency_wait() returns
+// once that predecessor has completed and its memory writes are visible, so
+// it comes before the kernel's first global access.  grid_launch_dependents()
+// lets the successor be scheduled once every CTA of this grid has called it
+// or exited.  Both do nothing for an ordinary launch.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Order-preserving map of a key's bits to an unsigned value (and back).
 // kind/desc are launch-uniform, so the selects compile to predicated ops.
 template <class U>

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
 
     for (int i = tid; i < G::NBINS * G::COPIES / 4; i += HIST_THREADS)
         reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
+    grid_launch_dependents();  // the first pass may be scheduled; it waits for this grid
 
     // Fused clears / copies that must precede the first pass.
     {
@@ -216,6 +217,12 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
     if constexpr (!G::HALF && rank_uses_or(IPT)) {
         for (int i = threadIdx.x; i < G::WARPS * 256; i += THREADS) match_scratch[i] = 0u;
     }
+    // Launched as a dependent of the previous kernel of the sort (plain mode):
+    // let the next one be scheduled, then wait for this one's inputs.  Every
+    // CTA of a pass is resident at once (grid <= SMs x occupancy), so the
+    // successor never holds slots a CTA of this pass still needs.
+    grid_launch_dependents();
+    grid_dependency_wait();
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // Tile position of item u of this thread: warp-striped (a warp's 32 lanes

@@ -94,6 +94,7 @@ __device__ void grid_copy_bytes(void* dst, const void* src, uint64_t bytes) {
 // After uniform-pass skipping: an odd number of executed passes left the
 // result in the alternate buffer; copy it home.  Otherwise nothing to do.
 __global__ void __launch_bounds__(256) skip_fixup_kernel(FixupParams f) {
+    grid_dependency_wait();  // launched as a dependent of the last pass
     // the executed pass kernels left their count; none ran when the word is 0
     const uint32_t w = *f.executed;
     const int executed = (w >> 31) ? int(w & 0xFFu) : 0;
@@ -212,6 +213,33 @@ int device_is_sm103() {
 // keep few CTAs: every CTA ends with one global atomic per digit bin, and at
 // 2^20 u32 keys 152 CTAs of 27 KB took 16.0 us against 12.2 us for 64 of
 // 64 KB.
+// Pass and fix-up launches of the plain sort are programmatic dependents of
+// the kernel before them (GBSORT_PDL=0 launches them ordinarily): the next
+// kernel is scheduled while the previous one drains, and waits in
+// grid_dependency_wait() for its results.
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("GBSORT_PDL");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+cudaError_t launch_dependent(const void* fn, uint32_t grid, int threads, size_t smem, cudaStream_t s, void** args) {
+    if (!pdl_enabled()) return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, s);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
 uint32_t upsweep_ctas(uint64_t n, int kb) {
     const uint64_t work = (n * uint64_t(kb) + HIST_THREADS * 64ull - 1) / (HIST_THREADS * 64ull);
     const uint64_t sms = uint64_t(device_sm_count() > 0 ? device_sm_count() : 1);
@@ -383,7 +411,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         pp.copy_vals_in = copy ? vals_src : nullptr;
         pp.executed = fixup ? reinterpret_cast<uint32_t*>(ctl + plan.ctl.exec_off) : nullptr;
         void* args[] = {&pp};
-        e = cudaLaunchKernel(plan.pass.fn, dim3(pass_ctas), dim3(plan.pass.threads), args, plan.pass.smem, stream);
+        e = launch_dependent(plan.pass.fn, pass_ctas, plan.pass.threads, plan.pass.smem, stream, args);
         if (e != cudaSuccess) return fail("pass launch", e);
         if (timed) cudaEventRecord(ev[2 + pass], stream);
     }
@@ -400,8 +428,8 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         fp.copy_keys_in = copy ? keys_src : nullptr;
         fp.copy_vals_in = copy ? vals_src : nullptr;
         void* args[] = {&fp};
-        e = cudaLaunchKernel(reinterpret_cast<const void*>(&skip_fixup_kernel), dim3(uint32_t(sms > 0 ? sms : 1)),
-                             dim3(256), args, 0, stream);
+        e = launch_dependent(reinterpret_cast<const void*>(&skip_fixup_kernel), uint32_t(sms > 0 ? sms : 1), 256, 0,
+                             stream, args);
         if (e != cudaSuccess) return fail("fixup launch", e);
         if (timed) cudaEventRecord(ev[2 + plan.passes], stream);
     }
