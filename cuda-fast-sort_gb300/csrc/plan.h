@@ -58,13 +58,23 @@ struct Plan {
 // Fills *plan; returns a gbsort_status code.
 int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan);
 
+// DoubleBuffer form: the caller's second key (and value) buffer replaces
+// the workspace's alternate buffers, and the workspace holds only the
+// control block and the lookback status (double_buffer_bytes).  The result
+// lands in the second buffer when the pass count is odd, else in the first.
+struct AltBuffers {
+    void* keys_b;
+    void* vals_b;
+};
+size_t double_buffer_bytes(const Plan& plan);
+
 // Enqueues one sort on `stream`.  `ms` (optional) receives per-kernel event
 // times after a stream sync: [upsweep, pass 0 .. pass P-1].
 // keys_src != nullptr: input-preserving sort, reads keys_src (and vals_src)
 // and leaves the result in d_keys (and d_values).
 int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values, void* d_workspace,
                  cudaStream_t stream, float* ms, int ms_cap, int* n_ms, const void* keys_src = nullptr,
-                 const void* vals_src = nullptr);
+                 const void* vals_src = nullptr, const AltBuffers* alt = nullptr);
 
 // Device facts (cached per device).
 int device_sm_count();

@@ -91,8 +91,9 @@ __device__ void grid_copy_bytes(void* dst, const void* src, uint64_t bytes) {
         static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
 }
 
-// After uniform-pass skipping: an odd number of executed passes left the
-// result in the alternate buffer; copy it home.  Otherwise nothing to do.
+// After uniform-pass skipping: the executed passes' parity left the result
+// in the other buffer than the one it belongs in (in place: an odd count
+// left it in the alternate buffer); copy it across.  Otherwise nothing to do.
 __global__ void __launch_bounds__(256) skip_fixup_kernel(FixupParams f) {
     grid_dependency_wait();  // launched as a dependent of the last pass
     // the executed pass kernels left their count; none ran when the word is 0
@@ -104,9 +105,11 @@ __global__ void __launch_bounds__(256) skip_fixup_kernel(FixupParams f) {
         if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.copy_vals_in, f.val_bytes_total);
         return;
     }
-    if ((executed & 1) == 0) return;
-    grid_copy_bytes(f.keys_a, f.keys_b, f.key_bytes_total);
-    if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.vals_b, f.val_bytes_total);
+    if ((executed & 1) == f.want_odd) return;
+    // the result sits in b after an odd number of executed passes, else in a
+    const bool in_b = (executed & 1) != 0;
+    grid_copy_bytes(in_b ? f.keys_a : f.keys_b, in_b ? f.keys_b : f.keys_a, f.key_bytes_total);
+    if (f.val_bytes_total) grid_copy_bytes(in_b ? f.vals_a : f.vals_b, in_b ? f.vals_b : f.vals_a, f.val_bytes_total);
 }
 thread_local std::string g_last_error;
 
@@ -301,9 +304,11 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     return GBSORT_OK;
 }
 
+size_t double_buffer_bytes(const Plan& plan) { return plan.total_bytes - plan.ctl_off; }
+
 int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values, void* d_workspace,
                  cudaStream_t stream, float* ms, int ms_cap, int* n_ms, const void* keys_src,
-                 const void* vals_src) {
+                 const void* vals_src, const AltBuffers* alt) {
     if (n_ms) *n_ms = 0;
     if (plan.n == 0) return GBSORT_OK;
     if (reinterpret_cast<uintptr_t>(d_workspace) % 16) {  // the status array is cleared by 16-byte stores
@@ -317,21 +322,27 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     if (st != GBSORT_OK) return st;
 
     uint8_t* ws = static_cast<uint8_t*>(d_workspace);
-    uint8_t* ctl = ws + plan.ctl_off;
+    // a DoubleBuffer workspace starts at the control block
+    const size_t ws_base = alt ? plan.ctl_off : 0;
+    uint8_t* ctl = ws + plan.ctl_off - ws_base;
     unsigned long long* gp = reinterpret_cast<unsigned long long*>(ctl + plan.ctl.gp_off);
     uint32_t* counters = reinterpret_cast<uint32_t*>(ctl + plan.ctl.counters_off);
     uint32_t* err_word = reinterpret_cast<uint32_t*>(ctl + plan.ctl.err_off);
-    void* status = ws + plan.status_off;
-    void* alt_keys = ws + plan.alt_keys_off;
-    void* alt_vals = plan.vb ? ws + plan.alt_vals_off : nullptr;
+    void* status = ws + plan.status_off - ws_base;
+    void* alt_keys = alt ? alt->keys_b : ws + plan.alt_keys_off;
+    void* alt_vals = plan.vb ? (alt ? alt->vals_b : ws + plan.alt_vals_off) : nullptr;
     const bool copy = keys_src != nullptr;  // input-preserving: read keys_src/vals_src, write d_keys/d_values
-    const bool odd = !copy && (plan.passes & 1) != 0;
+    // in place, odd pass counts start from a mirror so that they end at home;
+    // the DoubleBuffer form lets them end in the second buffer instead
+    const bool odd = !copy && !alt && (plan.passes & 1) != 0;
     const int sms = device_sm_count();
 
     const bool skip = g_pass_skip.load(std::memory_order_relaxed) != 0;
     // odd pass counts start mirrored and always end at home; an
-    // input-preserving sort needs the copy only when every pass was skipped
-    const bool fixup = skip && ((plan.passes & 1) == 0 || copy);
+    // input-preserving sort needs the copy only when every pass was skipped;
+    // a DoubleBuffer sort when the executed passes' parity differs from the
+    // pass count's
+    const bool fixup = skip && (alt != nullptr || (plan.passes & 1) == 0 || copy);
     const int nev = plan.passes + 2 + (fixup ? 1 : 0);
     cudaEvent_t ev[20] = {};
     const bool timed = ms != nullptr;
@@ -427,6 +438,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         fp.val_bytes_total = plan.vb ? plan.n * uint64_t(plan.vb) : 0;
         fp.copy_keys_in = copy ? keys_src : nullptr;
         fp.copy_vals_in = copy ? vals_src : nullptr;
+        fp.want_odd = alt ? (plan.passes & 1) : 0;
         void* args[] = {&fp};
         e = launch_dependent(reinterpret_cast<const void*>(&skip_fixup_kernel), uint32_t(sms > 0 ? sms : 1), 256, 0,
                              stream, args);
@@ -489,9 +501,12 @@ struct GraphKey {
     int device, key_type, desc, skip;
     size_t vb;
     uint64_t n, wait_limit;
-    const void *keys, *vals, *ws, *ksrc, *vsrc;
+    const void *keys, *vals, *ws, *ksrc, *vsrc, *keys_b, *vals_b;
     cudaStream_t stream;
-    auto tie() const { return std::tie(device, key_type, desc, skip, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc, stream); }
+    auto tie() const {
+        return std::tie(device, key_type, desc, skip, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc, keys_b, vals_b,
+                        stream);
+    }
     bool operator==(const GraphKey& o) const { return tie() == o.tie(); }
 };
 struct GraphEntry {
@@ -511,8 +526,10 @@ std::atomic<int> g_graph_cache{[] {
 }()};
 
 int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* ws, cudaStream_t s,
-                const void* ksrc, const void* vsrc) {
-    auto direct = [&] { return enqueue_sort(plan, descending, keys, vals, ws, s, nullptr, 0, nullptr, ksrc, vsrc); };
+                const void* ksrc, const void* vsrc, const AltBuffers* alt = nullptr) {
+    auto direct = [&] {
+        return enqueue_sort(plan, descending, keys, vals, ws, s, nullptr, 0, nullptr, ksrc, vsrc, alt);
+    };
     if (!g_graph_cache.load(std::memory_order_relaxed) || s == nullptr) return direct();
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
@@ -533,6 +550,8 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
     k.ws = ws;
     k.ksrc = ksrc;
     k.vsrc = vsrc;
+    k.keys_b = alt ? alt->keys_b : nullptr;
+    k.vals_b = alt ? alt->vals_b : nullptr;
     k.stream = s;
     std::lock_guard<std::mutex> lk(g_graph_mu);
     GraphEntry* e = nullptr;
@@ -618,6 +637,45 @@ bool ranges_overlap(const void* a, const void* b, size_t bytes) {
 // Input-preserving form: keys_in/vals_in are only read, the result goes to
 // keys_out/vals_out.  Identical input and output buffers mean in place;
 // any other overlap is refused.
+// DoubleBuffer form: buffers[*selector] holds the input; the passes
+// ping-pong between the two buffers; *selector names the result on return.
+int sort_double_common(int key_type, int descending, void* keys0, void* keys1, void* vals0, void* vals1,
+                       size_t value_bytes, int* selector, size_t* temp_bytes, void* d_workspace, size_t n,
+                       void* stream) {
+    int st = check_args(key_type, value_bytes, keys0, vals0, temp_bytes);
+    if (st != GBSORT_OK) return st;
+    if (selector == nullptr || (*selector != 0 && *selector != 1)) return GBSORT_ERR_INVALID_ARGUMENT;
+    Plan plan;
+    st = make_plan(key_type, value_bytes, n, &plan);
+    if (st != GBSORT_OK) return st;
+    if (d_workspace == nullptr) {
+        *temp_bytes = double_buffer_bytes(plan);
+        return GBSORT_OK;
+    }
+    if (n == 0) return GBSORT_OK;
+    if (keys0 == nullptr || keys1 == nullptr || (value_bytes != 0 && (vals0 == nullptr || vals1 == nullptr)))
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    const size_t kbytes = n * size_t(plan.kb), vbytes = n * value_bytes;
+    if (ranges_overlap(keys0, keys1, kbytes) || (value_bytes && ranges_overlap(vals0, vals1, vbytes))) {
+        set_last_error_text("the two buffers of a DoubleBuffer sort overlap");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
+    if (!naturally_aligned(keys0, size_t(plan.kb)) || !naturally_aligned(keys1, size_t(plan.kb)) ||
+        !naturally_aligned(vals0, value_bytes) || !naturally_aligned(vals1, value_bytes)) {
+        set_last_error_text("keys and values must be aligned to their own size");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
+    if (*temp_bytes < double_buffer_bytes(plan)) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    const int sel = *selector;
+    void* ka = sel ? keys1 : keys0;
+    void* va = value_bytes ? (sel ? vals1 : vals0) : nullptr;
+    AltBuffers alt{sel ? keys0 : keys1, value_bytes ? (sel ? vals0 : vals1) : nullptr};
+    st = launch_sort(plan, descending ? 1 : 0, ka, va, d_workspace, static_cast<cudaStream_t>(stream), nullptr,
+                     nullptr, &alt);
+    if (st == GBSORT_OK) *selector = sel ^ (plan.passes & 1);
+    return st;
+}
+
 int sort_copy_common(int key_type, int descending, const void* keys_in, void* keys_out, const void* vals_in,
                      void* vals_out, size_t value_bytes, size_t* temp_bytes, void* d_workspace, size_t n,
                      void* stream) {
@@ -668,6 +726,19 @@ int gbsort_sort_pairs_copy(int key_type, int descending, const void* d_keys_in, 
                            void* d_workspace, size_t n, void* stream) {
     return sort_copy_common(key_type, descending, d_keys_in, d_keys_out, d_values_in, d_values_out, value_bytes,
                             temp_bytes, d_workspace, n, stream);
+}
+
+int gbsort_sort_keys_double_buffer(int key_type, int descending, void* d_keys0, void* d_keys1, int* selector,
+                                   size_t* temp_bytes, void* d_workspace, size_t n, void* stream) {
+    return sort_double_common(key_type, descending, d_keys0, d_keys1, nullptr, nullptr, 0, selector, temp_bytes,
+                              d_workspace, n, stream);
+}
+
+int gbsort_sort_pairs_double_buffer(int key_type, int descending, void* d_keys0, void* d_keys1, void* d_values0,
+                                    void* d_values1, size_t value_bytes, int* selector, size_t* temp_bytes,
+                                    void* d_workspace, size_t n, void* stream) {
+    return sort_double_common(key_type, descending, d_keys0, d_keys1, d_values0, d_values1, value_bytes, selector,
+                              temp_bytes, d_workspace, n, stream);
 }
 
 size_t gbsort_key_bytes(int key_type) {
@@ -733,25 +804,37 @@ GBSORT_DEFINE_TYPED(f64, GBSORT_KEY_F64)
 GBSORT_DEFINE_TYPED(f128, GBSORT_KEY_F128)
 #undef GBSORT_DEFINE_TYPED
 
-int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {
-    Plan plan;
-    int st = make_plan(key_type, value_bytes, n, &plan);
-    if (st != GBSORT_OK) return st;
+namespace {
+// Synchronizes `stream` and decodes the error word of a workspace whose
+// control block starts `ctl_at` bytes in.
+int read_status(const Plan& plan, size_t ctl_at, void* d_workspace, void* stream) {
     if (d_workspace == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
-    if (n == 0) return GBSORT_OK;
+    if (plan.n == 0) return GBSORT_OK;
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) {
         set_last_error("stream sync", e);
         return GBSORT_ERR_CUDA;
     }
     uint32_t err = 0;
-    e = cudaMemcpy(&err, static_cast<uint8_t*>(d_workspace) + plan.ctl_off + plan.ctl.err_off, 4,
-                   cudaMemcpyDeviceToHost);
+    e = cudaMemcpy(&err, static_cast<uint8_t*>(d_workspace) + ctl_at + plan.ctl.err_off, 4, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
         set_last_error("status read", e);
         return GBSORT_ERR_CUDA;
     }
     return status_from_error_word(err);
+}
+}  // namespace
+
+int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {
+    Plan plan;
+    const int st = make_plan(key_type, value_bytes, n, &plan);
+    return st != GBSORT_OK ? st : read_status(plan, plan.ctl_off, d_workspace, stream);
+}
+
+int gbsort_double_buffer_status(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {
+    Plan plan;
+    const int st = make_plan(key_type, value_bytes, n, &plan);
+    return st != GBSORT_OK ? st : read_status(plan, 0, d_workspace, stream);
 }
 
 int gbsort_workspace_reset(int key_type, size_t value_bytes, size_t n, void* d_workspace, void* stream) {

@@ -80,12 +80,16 @@ struct PassParams {
 struct FixupParams {
     const uint32_t* executed;  // bit 31 | executed passes, 0 when none ran
     int passes;
-    const void* keys_b;
+    void* keys_b;
     void* keys_a;
     uint64_t key_bytes_total;
-    const void* vals_b;
+    void* vals_b;
     void* vals_a;
     uint64_t val_bytes_total;
+    // parity of executed passes that leaves the result where it belongs:
+    // 0 in place (in a), 1 in b (DoubleBuffer form of an odd pass count);
+    // otherwise the result is copied across
+    int want_odd;
     // input-preserving sort: when no pass ran, copy these to the output
     const void* copy_keys_in;
     const void* copy_vals_in;

@@ -575,6 +575,54 @@ def sort_copy(keys_in, keys_out, n: int, key_type, workspace, workspace_bytes: i
     _check(st, "sort copy")
 
 
+def _double_buffer_fn(value_bytes: int):
+    l = lib()
+    vp, sz, i = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+    ip, tp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t)
+    if value_bytes:
+        f = l.gbsort_sort_pairs_double_buffer
+        f.argtypes = [i, i, vp, vp, vp, vp, sz, ip, tp, vp, sz, vp]
+    else:
+        f = l.gbsort_sort_keys_double_buffer
+        f.argtypes = [i, i, vp, vp, ip, tp, vp, sz, vp]
+    f.restype = i
+    return f
+
+
+def double_buffer_bytes(key_type, n: int, value_bytes: int = 0) -> int:
+    """Workspace bytes of the DoubleBuffer form (control words and status only)."""
+    f = _double_buffer_fn(value_bytes)
+    tb = ctypes.c_size_t(0)
+    sel = ctypes.c_int(0)
+    args = [key_type_id(key_type), 0, None, None] + ([None, None, value_bytes] if value_bytes else [])
+    _check(f(*args, ctypes.byref(sel), ctypes.byref(tb), None, n, None), "size query")
+    return tb.value
+
+
+def sort_double_buffer(keys0, keys1, n: int, key_type, workspace, workspace_bytes: int, *, selector: int = 0,
+                       values0=None, values1=None, value_bytes: int = 0, descending: bool = False,
+                       stream=None) -> int:
+    """DoubleBuffer sort (gbsort_sort_keys/pairs_double_buffer): the input is
+    in buffer `selector` (0: keys0/values0, 1: keys1/values1); returns the
+    selector of the buffer holding the result."""
+    f = _double_buffer_fn(value_bytes)
+    tb = ctypes.c_size_t(workspace_bytes)
+    sel = ctypes.c_int(selector)
+    vals = [_ptr(values0), _ptr(values1), value_bytes] if value_bytes else []
+    st = f(key_type_id(key_type), int(descending), _ptr(keys0), _ptr(keys1), *vals, ctypes.byref(sel),
+           ctypes.byref(tb), _ptr(workspace), n, _stream(stream))
+    _check(st, "double-buffer sort")
+    return sel.value
+
+
+def double_buffer_status(key_type, n: int, workspace, value_bytes: int = 0, stream=None) -> int:
+    """gbsort_double_buffer_status: syncs `stream`, returns the last DoubleBuffer sort's status."""
+    f = lib().gbsort_double_buffer_status
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    return f(key_type_id(key_type), value_bytes, n, _ptr(workspace), _stream(stream))
+
+
 # ---- device-side result checks ------------------------------------------------
 
 def check_order(keys, n: int, key_type, descending: bool = False, stream=None) -> int:

@@ -121,6 +121,32 @@ int gbsort_sort_pairs_copy(int key_type, int descending, const void* d_keys_in,
                            size_t* temp_bytes, void* d_workspace, size_t n,
                            void* stream);
 
+/* DoubleBuffer forms, as cub::DoubleBuffer in the reference's CUB comparator
+ * (benchmark/cub_radix_double.cu:79-111): the caller owns two key buffers
+ * (and two value buffers) of n elements; *selector (0 or 1) names the one
+ * holding the input and, on return, the one holding the sorted result
+ * (flipped when the key has an odd number of bytes' passes, i.e. 1-byte
+ * keys).  The passes ping-pong between the caller's buffers, so the
+ * workspace holds only control words and lookback status, not n-sized
+ * alternate buffers (2^28 u32 keys: ~30 MB instead of ~1.1 GB).  The other
+ * buffer is clobbered.  d_workspace == NULL writes the required bytes to
+ * *temp_bytes (no device work).  The buffers of a pair must not overlap. */
+int gbsort_sort_keys_double_buffer(int key_type, int descending, void* d_keys0,
+                                   void* d_keys1, int* selector,
+                                   size_t* temp_bytes, void* d_workspace,
+                                   size_t n, void* stream);
+int gbsort_sort_pairs_double_buffer(int key_type, int descending,
+                                    void* d_keys0, void* d_keys1,
+                                    void* d_values0, void* d_values1,
+                                    size_t value_bytes, int* selector,
+                                    size_t* temp_bytes, void* d_workspace,
+                                    size_t n, void* stream);
+/* gbsort_workspace_status for a DoubleBuffer workspace (its control block
+ * sits at the start): synchronizes `stream`, then reports a timed-out wait
+ * or a failed bounds check of the last sort that used it. */
+int gbsort_double_buffer_status(int key_type, size_t value_bytes, size_t n,
+                                void* d_workspace, void* stream);
+
 /* Typed convenience entry points (same semantics as above). */
 #define GBSORT_DECLARE_TYPED(name)                                              \
     int gbsort_sort_##name(void* d_keys, size_t* temp_bytes, void* d_workspace, \

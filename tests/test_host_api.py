@@ -53,3 +53,29 @@ def test_status_strings(gb):
     for st in range(9):
         assert gb.status_string(st) and gb.status_string(st) != "unknown status"
     assert gb.status_string(99) == "unknown status"
+
+
+@pytest.mark.parametrize("kt,vb", [("u8", 0), ("u32", 0), ("u32", 4), ("u64", 8), ("u128", 16)])
+def test_double_buffer_size_query(gb, kt, vb):
+    """The DoubleBuffer workspace holds control words and status only."""
+    kb = KEY_BYTES[kt]
+    for n in (0, 1, 5000, 1 << 22, 1 << 28):
+        db = gb.double_buffer_bytes(kt, n, vb)
+        assert 0 < db <= gb.temp_bytes(kt, n, vb) - n * (kb + vb) + 512
+        if n:
+            assert db < gb.temp_bytes(kt, n, vb)
+    if kt == "u32" and vb == 0:  # 2^28 keys: ~30 MB instead of ~1.1 GB
+        assert gb.double_buffer_bytes(kt, 1 << 28) < 32 << 20
+
+
+def test_double_buffer_rejects_bad_selector(gb):
+    l = gb.lib()
+    f = l.gbsort_sort_keys_double_buffer
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                  ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    tb = ctypes.c_size_t(0)
+    for bad in (2, -1):
+        sel = ctypes.c_int(bad)
+        assert f(2, 0, None, None, ctypes.byref(sel), ctypes.byref(tb), None, 10, None) == gb.ERR_INVALID_ARGUMENT
+    assert f(2, 0, None, None, None, ctypes.byref(tb), None, 10, None) == gb.ERR_INVALID_ARGUMENT
