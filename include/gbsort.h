@@ -124,9 +124,8 @@ int gbsort_sort_pairs_copy(int key_type, int descending, const void* d_keys_in,
 /* DoubleBuffer forms, as cub::DoubleBuffer in the reference's CUB comparator
  * (benchmark/cub_radix_double.cu:79-111): the caller owns two key buffers
  * (and two value buffers) of n elements; *selector (0 or 1) names the one
- * holding the input and, on return, the one holding the sorted result
- * (flipped when the key has an odd number of bytes' passes, i.e. 1-byte
- * keys).  The passes ping-pong between the caller's buffers, so the
+ * holding the input and, on return, the one holding the sorted result (it
+ * flips only for 1-byte keys, whose sort is a single pass).  The passes ping-pong between the caller's buffers, so the
  * workspace holds only control words and lookback status, not n-sized
  * alternate buffers (2^28 u32 keys: ~30 MB instead of ~1.1 GB).  The other
  * buffer is clobbered.  d_workspace == NULL writes the required bytes to
