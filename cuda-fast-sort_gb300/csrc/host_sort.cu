@@ -35,8 +35,10 @@
 #include "plan.h"
 #include "device_common.cuh"
 #include "sort_params.h"
+#include "segmented_internal.h"
 
 namespace gbsort {
+
 namespace {
 
 uint64_t env_u64(const char* name, uint64_t dflt) {
@@ -93,18 +95,20 @@ size_t plain_bytes(const Plan& p, size_t vb) {
     return off + p.total_bytes;
 }
 
-// One non-blocking copy stream per device, created on first use.
-cudaStream_t copy_stream() {
+// Two non-blocking copy streams per device (0: the host sort's copies and
+// the batched copies in, 1: the batched copies out), created on first use.
+cudaStream_t copy_stream(int which = 0) {
     static std::mutex mu;
-    static cudaStream_t streams[64] = {};
+    static cudaStream_t streams[64][2] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     std::lock_guard<std::mutex> lk(mu);
-    if (streams[dev] == nullptr && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStream_t& st = streams[dev][which & 1];
+    if (st == nullptr && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
-        streams[dev] = nullptr;
+        st = nullptr;
     }
-    return streams[dev];
+    return st;
 }
 
 uint32_t pass_ctas(const Plan& p) {
@@ -379,6 +383,223 @@ int sort_host_split(const Plan& P, int key_type, int desc, uint8_t* h_keys, uint
     return finish(status_from_error_word(w));
 }
 
+// ---- batched sort from host memory ----------------------------------------
+// Consecutive segments form about GBSORT_HOST_SPLIT_GROUPS groups of ~n/16
+// keys (a segment is never split).  Group g+1's keys come in on one copy
+// stream while group g sorts (one batched run per group, on the caller's
+// stream) and group g-1 goes back on the other copy stream, so both
+// directions of the host link work at once.
+
+struct SegGroup {
+    size_t first = 0, end = 0;  // segments [first, end)
+    gbsort_segmented_plan* plan = nullptr;
+    size_t ws_bytes = 0, image_bytes = 0, image_off = 0;
+};
+
+struct SegHostJob {
+    std::vector<SegGroup> groups;
+    size_t ws_max = 0, image_total = 0;
+    // d_buffer: [keys][values][error words][every group's tables][workspace]
+    size_t stage_keys = 0, stage_vals = 0, errs = 0, tables = 0, ws = 0, total = 0;
+    ~SegHostJob() {
+        for (SegGroup& g : groups)
+            if (g.plan) gbsort_segmented_plan_destroy(g.plan);
+    }
+};
+
+int seg_host_job(int key_type, size_t vb, int desc, const uint64_t* off, size_t num, SegHostJob* job) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    if (kb == 0 || (num > 0 && off == nullptr)) return GBSORT_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < num; ++i)
+        if (off[i + 1] < off[i]) return GBSORT_ERR_INVALID_ARGUMENT;
+    const uint64_t n = num ? off[num] - off[0] : 0;
+    const int G = split_groups();
+    const uint64_t target = std::max<uint64_t>(1, (n + uint64_t(G) - 1) / uint64_t(G));
+    size_t first = 0;
+    for (size_t i = 0; i < num; ++i) {
+        if (off[i + 1] - off[first] >= target || i + 1 == num) {
+            SegGroup g;
+            g.first = first;
+            g.end = i + 1;
+            job->groups.push_back(g);
+            first = i + 1;
+        }
+    }
+    std::vector<uint64_t> rel;
+    for (SegGroup& g : job->groups) {
+        rel.assign(off + g.first, off + g.end + 1);
+        for (uint64_t& x : rel) x -= off[g.first];
+        int st = gbsort_segmented_plan_create(key_type, vb, desc, rel.data(), g.end - g.first, &g.plan);
+        if (st != GBSORT_OK) return st;
+        gbsort_segmented_info info{};
+        st = gbsort_segmented_plan_info(g.plan, &info);
+        if (st != GBSORT_OK) return st;
+        g.ws_bytes = size_t(info.workspace_bytes);
+        g.image_bytes = segmented_table_bytes(g.plan);
+        g.image_off = job->image_total;
+        job->image_total += align_up(g.image_bytes, 256);
+        job->ws_max = std::max(job->ws_max, g.ws_bytes);
+    }
+    job->stage_keys = 0;
+    job->stage_vals = align_up(size_t(n) * kb, 256);
+    job->errs = job->stage_vals + align_up(size_t(n) * vb, 256);
+    job->tables = job->errs + align_up(std::max<size_t>(1, job->groups.size()) * 4, 256);
+    job->ws = job->tables + align_up(job->image_total, 256);
+    job->total = job->ws + align_up(job->ws_max, 256);
+    return GBSORT_OK;
+}
+
+// Pinned host memory for the groups' table images, kept between calls.
+struct PinnedImages {
+    std::mutex mu;
+    uint8_t* buf = nullptr;
+    size_t cap = 0;
+};
+PinnedImages& pinned_images() {
+    static PinnedImages p;
+    return p;
+}
+
+int sort_segmented_host(int key_type, int desc, uint8_t* h_keys, uint8_t* h_vals, size_t vb, const uint64_t* off,
+                        SegHostJob& job, uint8_t* base, cudaStream_t s) {
+    const size_t kb = gbsort_key_bytes(key_type);
+    const uint64_t off0 = off[0];
+    uint8_t* stage_k = base + job.stage_keys;
+    uint8_t* stage_v = vb ? base + job.stage_vals : nullptr;
+    uint8_t* ws = base + job.ws;
+    uint8_t* tables = base + job.tables;
+    uint32_t* errs = reinterpret_cast<uint32_t*>(base + job.errs);
+    cudaStream_t cin = copy_stream(0), cout = copy_stream(1);
+    if (cin == nullptr || cout == nullptr) {
+        set_last_error_text("batched host sort: no copy stream");
+        return GBSORT_ERR_CUDA;
+    }
+    PinnedImages& pi = pinned_images();
+    std::lock_guard<std::mutex> lk(pi.mu);  // the images stay in use until this call returns
+    if (job.image_total > pi.cap) {
+        if (pi.buf) cudaFreeHost(pi.buf);
+        pi.buf = nullptr;
+        pi.cap = 0;
+        const cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&pi.buf), job.image_total, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            pi.buf = nullptr;
+            set_last_error("batched host sort: table images", e);
+            return GBSORT_ERR_CUDA;
+        }
+        pi.cap = job.image_total;
+    }
+    for (const SegGroup& g : job.groups)
+        if (g.image_bytes) segmented_table_image(g.plan, pi.buf + g.image_off);
+
+    std::vector<cudaEvent_t> evs;
+    auto event = [&](cudaEvent_t* ev) {
+        const cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) evs.push_back(*ev);
+        return e;
+    };
+    // GBSORT_HOST_TRACE=1: device times of the phases, printed on stderr
+    const bool trace = env_u64("GBSORT_HOST_TRACE", 0) == 1;
+    std::vector<std::pair<std::string, cudaEvent_t>> marks;
+    auto mark = [&](const std::string& label, cudaStream_t st) {
+        if (!trace) return;
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        evs.push_back(ev);
+        cudaEventRecord(ev, st);
+        marks.emplace_back(label, ev);
+    };
+    auto finish = [&](int status) {
+        if (trace && !marks.empty()) {
+            std::fprintf(stderr, "gbsort-host batched groups=%zu\n", job.groups.size());
+            for (const auto& m : marks) {
+                float t = 0.f;
+                if (cudaEventElapsedTime(&t, marks[0].second, m.second) != cudaSuccess) cudaGetLastError();
+                std::fprintf(stderr, "  %-28s %9.3f ms\n", m.first.c_str(), double(t));
+            }
+        }
+        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+        return status;
+    };
+    auto fail = [&](const char* what, cudaError_t e, int status) {
+        if (e != cudaSuccess) set_last_error(what, e);
+        // nothing of this call may still run when it returns
+        cudaStreamSynchronize(cin);
+        cudaStreamSynchronize(s);
+        cudaStreamSynchronize(cout);
+        cudaGetLastError();
+        return finish(status);
+    };
+    const size_t G = job.groups.size();
+    cudaError_t e = cudaMemsetAsync(errs, 0, G * 4, s);
+    cudaEvent_t ev_start;
+    if (e == cudaSuccess) e = event(&ev_start);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_start, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cin, ev_start, 0);
+    if (e != cudaSuccess) return fail("batched host sort", e, GBSORT_ERR_CUDA);
+    mark("start", s);
+    // every group's tables first (one small copy), then every group's keys:
+    // a group's tables then reach its workspace by a kernel, which cannot
+    // queue behind the bulk copies on the copy engine
+    cudaEvent_t tables_in;
+    if ((e = event(&tables_in)) != cudaSuccess) return fail("batched host sort event", e, GBSORT_ERR_CUDA);
+    if (job.image_total) e = cudaMemcpyAsync(tables, pi.buf, job.image_total, cudaMemcpyHostToDevice, cin);
+    if (e == cudaSuccess) e = cudaEventRecord(tables_in, cin);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tables_in, 0);
+    if (e != cudaSuccess) return fail("batched host sort tables", e, GBSORT_ERR_CUDA);
+    std::vector<cudaEvent_t> in(G), done(G);
+    for (size_t i = 0; i < G; ++i) {
+        const SegGroup& g = job.groups[i];
+        const uint64_t at = off[g.first] - off0, m = off[g.end] - off[g.first];
+        if ((e = event(&in[i])) != cudaSuccess) return fail("batched host sort event", e, GBSORT_ERR_CUDA);
+        if (m) e = cudaMemcpyAsync(stage_k + at * kb, h_keys + (off0 + at) * kb, m * kb, cudaMemcpyHostToDevice, cin);
+        if (e == cudaSuccess && m && vb)
+            e = cudaMemcpyAsync(stage_v + at * vb, h_vals + (off0 + at) * vb, m * vb, cudaMemcpyHostToDevice, cin);
+        if (e == cudaSuccess) e = cudaEventRecord(in[i], cin);
+        if (e != cudaSuccess) return fail("batched host sort copy in", e, GBSORT_ERR_CUDA);
+        mark("group " + std::to_string(i) + " in", cin);
+    }
+    for (size_t i = 0; i < G; ++i) {
+        const SegGroup& g = job.groups[i];
+        const uint64_t at = off[g.first] - off0;
+        if ((e = cudaStreamWaitEvent(s, in[i], 0)) != cudaSuccess)
+            return fail("batched host sort", e, GBSORT_ERR_CUDA);
+        int st = segmented_bind_image(g.plan, stage_k + at * kb, stage_v ? stage_v + at * vb : nullptr, ws,
+                                      job.ws_max, s, tables + g.image_off, true);
+        if (st == GBSORT_OK) st = gbsort_segmented_run(g.plan, 0, s);
+        if (st != GBSORT_OK) return fail("batched host sort", cudaSuccess, st);
+        e = cudaMemcpyAsync(errs + i, segmented_error_word(g.plan), 4, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = event(&done[i]);
+        if (e == cudaSuccess) e = cudaEventRecord(done[i], s);
+        if (e != cudaSuccess) return fail("batched host sort", e, GBSORT_ERR_CUDA);
+        mark("group " + std::to_string(i) + " sorted", s);
+    }
+    // copies back last: one into pageable memory blocks the host, and every
+    // sort must already be queued by then
+    for (size_t i = 0; i < G; ++i) {
+        const SegGroup& g = job.groups[i];
+        const uint64_t at = off[g.first] - off0, m = off[g.end] - off[g.first];
+        e = cudaStreamWaitEvent(cout, done[i], 0);
+        if (e == cudaSuccess && m)
+            e = cudaMemcpyAsync(h_keys + (off0 + at) * kb, stage_k + at * kb, m * kb, cudaMemcpyDeviceToHost, cout);
+        if (e == cudaSuccess && m && vb)
+            e = cudaMemcpyAsync(h_vals + (off0 + at) * vb, stage_v + at * vb, m * vb, cudaMemcpyDeviceToHost, cout);
+        if (e != cudaSuccess) return fail("batched host sort copy out", e, GBSORT_ERR_CUDA);
+        mark("group " + std::to_string(i) + " home", cout);
+    }
+    std::vector<uint32_t> w(G, 0);
+    e = cudaStreamSynchronize(cout);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.data(), errs, G * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail("batched host sort finish", e, GBSORT_ERR_CUDA);
+    uint32_t all = 0;
+    for (uint32_t x : w) all |= x;
+    return finish(status_from_error_word(all));
+}
+
 }  // namespace
 }  // namespace gbsort
 
@@ -442,6 +663,33 @@ int gbsort_sort_host(int key_type, int descending, void* h_keys, void* h_values,
         return GBSORT_ERR_CUDA;
     }
     return status_from_error_word(err);
+}
+
+size_t gbsort_segmented_host_buffer_bytes(int key_type, size_t value_bytes, const uint64_t* h_offsets,
+                                          size_t num_segments) {
+    SegHostJob job;
+    if (seg_host_job(key_type, value_bytes, 0, h_offsets, num_segments, &job) != GBSORT_OK) return 0;
+    return job.total;
+}
+
+int gbsort_segmented_sort_host(int key_type, int descending, void* h_keys, void* h_values, size_t value_bytes,
+                               const uint64_t* h_offsets, size_t num_segments, void* d_buffer, size_t buffer_bytes,
+                               void* stream) {
+    SegHostJob job;
+    int st = seg_host_job(key_type, value_bytes, descending ? 1 : 0, h_offsets, num_segments, &job);
+    if (st != GBSORT_OK) return st;
+    if (num_segments == 0 || h_offsets[num_segments] == h_offsets[0]) return GBSORT_OK;
+    if (h_keys == nullptr || d_buffer == nullptr || (value_bytes && h_values == nullptr))
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    if (buffer_bytes < job.total) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
+    if (reinterpret_cast<uintptr_t>(d_buffer) % 16) {  // holds a workspace: 16-byte stores clear its status array
+        set_last_error_text("the device buffer must be 16-byte aligned");
+        return GBSORT_ERR_INVALID_ARGUMENT;
+    }
+    if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
+    return sort_segmented_host(key_type, descending ? 1 : 0, static_cast<uint8_t*>(h_keys),
+                               static_cast<uint8_t*>(h_values), value_bytes, h_offsets, job,
+                               static_cast<uint8_t*>(d_buffer), static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -23,6 +23,7 @@
 #include "plan.h"
 #include "device_common.cuh"
 #include "sort_params.h"
+#include "segmented_internal.h"
 
 namespace gbsort {
 
@@ -494,8 +495,26 @@ void segmented_table_image(const gbsort_segmented_plan* p, uint8_t* dst) {
 
 // bind with the table image taken from `image` (pinned memory lets the
 // upload run asynchronously); image == nullptr builds it in pageable memory.
+namespace {
+// Copies a table image that is already in device memory into a workspace
+// (a kernel, not a copy engine: it cannot queue behind bulk transfers).
+__global__ void __launch_bounds__(256) table_copy_kernel(uint8_t* dst, const uint8_t* src, size_t bytes) {
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x, stride = size_t(gridDim.x) * blockDim.x;
+    size_t done = 0;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+        const size_t nv = bytes >> 4;
+        for (size_t i = t; i < nv; i += stride) reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
+        done = nv << 4;
+    }
+    for (size_t i = done + t; i < bytes; i += stride) dst[i] = src[i];
+}
+}  // namespace
+
+// image_on_device: `image` is a device copy of segmented_table_image(p),
+// moved into the workspace by a kernel; otherwise host memory (pinned, or
+// nullptr for the plan's own pageable image) uploaded on `stream`.
 int segmented_bind_image(gbsort_segmented_plan* p, void* d_keys, void* d_values, void* d_workspace,
-                         size_t workspace_bytes, void* stream, const uint8_t* image) {
+                         size_t workspace_bytes, void* stream, const uint8_t* image, bool image_on_device) {
     if (!p || (p->num_segments && !d_keys) || (p->vb && p->num_segments && !d_values)) return GBSORT_ERR_INVALID_ARGUMENT;
     if (d_workspace == nullptr || workspace_bytes < p->total_bytes) return GBSORT_ERR_WORKSPACE_TOO_SMALL;
     if (reinterpret_cast<uintptr_t>(d_workspace) % 16) {  // the status array is cleared by 16-byte stores
@@ -514,6 +533,17 @@ int segmented_bind_image(gbsort_segmented_plan* p, void* d_keys, void* d_values,
     // the tables sit back to back in the workspace: upload them as one image
     const size_t bytes = segmented_table_bytes(p);
     if (bytes == 0) return GBSORT_OK;
+    if (image_on_device) {
+        const uint32_t grid = uint32_t(std::min<size_t>((bytes + 4095) / 4096, 1024));
+        table_copy_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(p->ws + p->seg_begin_off, image,
+                                                                              bytes);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_last_error("segmented table copy", e);
+            return GBSORT_ERR_CUDA;
+        }
+        return GBSORT_OK;
+    }
     const uint8_t* src = image;
     if (src == nullptr) {  // kept with the plan: the copy may read it later
         p->image.resize(bytes);

@@ -42,14 +42,7 @@
 #include "gbsort.h"
 #include "plan.h"
 #include "device_common.cuh"
-
-namespace gbsort {
-const void* segmented_error_word(const gbsort_segmented_plan* p);
-size_t segmented_table_bytes(const gbsort_segmented_plan* p);
-void segmented_table_image(const gbsort_segmented_plan* p, uint8_t* dst);
-int segmented_bind_image(gbsort_segmented_plan* p, void* d_keys, void* d_values, void* d_workspace,
-                         size_t workspace_bytes, void* stream, const uint8_t* image);
-}
+#include "segmented_internal.h"
 
 namespace {
 

@@ -107,6 +107,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "gbsort_segmented_run": (i, [vp, i, vp]),
         "gbsort_segmented_status": (i, [vp, vp]),
         "gbsort_segmented_sort": (i, [i, i, vp, vp, sz, ctypes.POINTER(ctypes.c_uint64), sz, psz, vp, vp]),
+        "gbsort_segmented_host_buffer_bytes": (sz, [i, sz, ctypes.POINTER(ctypes.c_uint64), sz]),
+        "gbsort_segmented_sort_host": (i, [i, i, vp, vp, sz, ctypes.POINTER(ctypes.c_uint64), sz, vp, sz, vp]),
         "gbsort_set_segmented_path": (i, [i, sz, i, i]),
         "gbsort_get_segmented_path": (i, [i, sz, i]),
     })
@@ -328,6 +330,22 @@ def segmented_sort(keys, key_type, offsets, workspace=None, workspace_bytes: int
                                      ptr, len(off) - 1, ctypes.byref(tb), _ptr(workspace), _stream(stream))
     _check(st, "segmented sort")
     return tb.value
+
+
+def segmented_host_buffer_bytes(key_type, offsets, value_bytes: int = 0) -> int:
+    off, ptr = _offsets_array(offsets)
+    return lib().gbsort_segmented_host_buffer_bytes(key_type_id(key_type), value_bytes, ptr, len(off) - 1)
+
+
+def segmented_sort_host(h_keys, key_type, offsets, d_buffer, buffer_bytes: int, *, h_values=None,
+                        value_bytes: int = 0, descending: bool = False, stream=None) -> None:
+    """Batched sort of host-resident segments (pointers or pinned tensors),
+    copies overlapped with the sorting, through d_buffer."""
+    off, ptr = _offsets_array(offsets)
+    st = lib().gbsort_segmented_sort_host(key_type_id(key_type), int(descending), _ptr(h_keys), _ptr(h_values),
+                                          value_bytes if h_values is not None else 0, ptr, len(off) - 1,
+                                          _ptr(d_buffer), buffer_bytes, _stream(stream))
+    _check(st, "batched host sort")
 
 
 def set_segmented_path(key_type, value_bytes: int, size_log2: int, path: int) -> None:

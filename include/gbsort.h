@@ -268,6 +268,23 @@ int gbsort_segmented_sort(int key_type, int descending, void* d_keys,
                           void* d_values, size_t value_bytes,
                           const uint64_t* h_offsets, size_t num_segments,
                           size_t* temp_bytes, void* d_workspace, void* stream);
+/* Batched sort of segments in HOST memory (keys, values and offsets on the
+ * host; segment i is [h_offsets[i], h_offsets[i+1]) of h_keys): copies in,
+ * sorts every segment, copies back, then synchronizes.  Consecutive segments
+ * form about GBSORT_HOST_SPLIT_GROUPS (default 16) groups; a group's keys
+ * come in on one library-owned copy stream while the previous group sorts on
+ * `stream` and the one before goes back on a second copy stream, so both
+ * directions of the host link work at once (pinned memory for full speed).
+ * d_buffer (16-byte aligned) holds gbsort_segmented_host_buffer_bytes(...)
+ * bytes: the keys and values once plus one group's workspace. */
+size_t gbsort_segmented_host_buffer_bytes(int key_type, size_t value_bytes,
+                                          const uint64_t* h_offsets,
+                                          size_t num_segments);
+int gbsort_segmented_sort_host(int key_type, int descending, void* h_keys,
+                               void* h_values, size_t value_bytes,
+                               const uint64_t* h_offsets, size_t num_segments,
+                               void* d_buffer, size_t buffer_bytes,
+                               void* stream);
 /* Tuning table: the path segments of size [2^size_log2, 2^(size_log2+1))
  * take for this key type and value size (size_log2 = -1: every bucket;
  * path = -1: back to the built-in size thresholds).  A path too small for a
