@@ -10,8 +10,8 @@
 //      counted (upsweep) as soon as it lands; the counts are read back
 //   2. one onesweep pass on the top digit partitions half A of the buffer
 //      stably into the 256 buckets of half B
-//   3. consecutive buckets form about GBSORT_HOST_SPLIT_GROUPS (16) groups
-//      of ~n/16 keys; each group is sorted alone (upsweep + LSD passes over its
+//   3. consecutive buckets form groups of ~2^24 keys (2 to 16 groups;
+//      GBSORT_HOST_SPLIT_GROUPS overrides); each group is sorted alone (upsweep + LSD passes over its
 //      slice, alternating between B and A) on the caller's stream, and its
 //      slice goes back to the host on the copy stream as soon as its last
 //      pass is done, while the next groups sort.
@@ -20,7 +20,7 @@
 // top digit (its last pass).  Digits uniform over the whole array are
 // skipped (unless pass skipping is off); when the top digit puts more than
 // half of the keys into one bucket the partition is left out (one group,
-// every varying digit).  Arrays below GBSORT_HOST_SPLIT_MIN keys (2^24) and
+// every varying digit).  Arrays below GBSORT_HOST_SPLIT_MIN keys (2^25) and
 // 1-byte keys take the plain path: copy in, sort, copy back.
 
 #include <algorithm>
@@ -49,10 +49,16 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
     return (end != nullptr && *end == 0) ? uint64_t(x) : dflt;
 }
 
-uint64_t split_min_keys() { return env_u64("GBSORT_HOST_SPLIT_MIN", uint64_t(1) << 24); }
+// The split pays once each group is a sort of ~2^24 keys or more: smaller
+// sorts are latency-bound (2^20 keys: ~60 us), so 16 groups of 2^20 made a
+// 2^24-key call slower (1.64 ms against 0.99 ms plain), while 16 groups of
+// 2^24 keys take a 2^28-key call from 14.7 to 12.1 ms.
+uint64_t split_min_keys() { return env_u64("GBSORT_HOST_SPLIT_MIN", uint64_t(1) << 25); }
 
-int split_groups() {
-    const uint64_t g = env_u64("GBSORT_HOST_SPLIT_GROUPS", 16);
+// Groups for n keys: GBSORT_HOST_SPLIT_GROUPS, else one per 2^24 keys (2..16).
+int split_groups(uint64_t n) {
+    const uint64_t dflt = std::min<uint64_t>(16, std::max<uint64_t>(2, n >> 24));
+    const uint64_t g = env_u64("GBSORT_HOST_SPLIT_GROUPS", dflt);
     return int(g < 1 ? 1 : (g > 256 ? 256 : g));
 }
 
@@ -289,7 +295,8 @@ int sort_host_split(const Plan& P, int key_type, int desc, uint8_t* h_keys, uint
         mark("partitioned", s);
         src_k = B_k;
         src_v = B_v;
-        const uint64_t target = (n + uint64_t(split_groups()) - 1) / uint64_t(split_groups());
+        const int G = split_groups(n);
+        const uint64_t target = (n + uint64_t(G) - 1) / uint64_t(G);
         uint64_t at = 0, begin = 0;
         int first_bucket = -1;
         for (int d = 0; d < 256; ++d) {
@@ -384,8 +391,8 @@ int sort_host_split(const Plan& P, int key_type, int desc, uint8_t* h_keys, uint
 }
 
 // ---- batched sort from host memory ----------------------------------------
-// Consecutive segments form about GBSORT_HOST_SPLIT_GROUPS groups of ~n/16
-// keys (a segment is never split).  Group g+1's keys come in on one copy
+// Consecutive segments form groups of ~2^24 keys (2 to 16;
+// GBSORT_HOST_SPLIT_GROUPS overrides; a segment is never split).  Group g+1's keys come in on one copy
 // stream while group g sorts (one batched run per group, on the caller's
 // stream) and group g-1 goes back on the other copy stream, so both
 // directions of the host link work at once.
@@ -413,7 +420,7 @@ int seg_host_job(int key_type, size_t vb, int desc, const uint64_t* off, size_t 
     for (size_t i = 0; i < num; ++i)
         if (off[i + 1] < off[i]) return GBSORT_ERR_INVALID_ARGUMENT;
     const uint64_t n = num ? off[num] - off[0] : 0;
-    const int G = split_groups();
+    const int G = split_groups(n);
     const uint64_t target = std::max<uint64_t>(1, (n + uint64_t(G) - 1) / uint64_t(G));
     size_t first = 0;
     for (size_t i = 0; i < num; ++i) {

@@ -195,11 +195,11 @@ int gbsort_sort_keys_noalloc(int key_type, int descending, void* d_keys,
  * gbsort_host_buffer_bytes(...) bytes (twice the keys and values, plus
  * control words); pinned host memory gives full copy bandwidth.  No
  * allocation happens inside.  Arrays of >= GBSORT_HOST_SPLIT_MIN keys
- * (environment, default 2^24; keys of 2 bytes or more) are partitioned by
- * their top digit first and sorted in about GBSORT_HOST_SPLIT_GROUPS
- * (default 16) groups of consecutive buckets, each copied back on a
- * library-owned copy stream while the next ones sort; the work is ordered
- * after what `stream` already holds.  Smaller arrays are copied in, sorted
+ * (environment, default 2^25; keys of 2 bytes or more) are partitioned by
+ * their top digit first and sorted in groups of consecutive buckets of
+ * ~2^24 keys (2 to 16; GBSORT_HOST_SPLIT_GROUPS overrides), each copied
+ * back on a library-owned copy stream while the next ones sort; the work is
+ * ordered after what `stream` already holds.  Smaller arrays are copied in, sorted
  * and copied back on `stream`.  Either way the result is the in-place sort's. */
 size_t gbsort_host_buffer_bytes(int key_type, size_t value_bytes, size_t n);
 int gbsort_sort_host(int key_type, int descending, void* h_keys,
@@ -271,7 +271,8 @@ int gbsort_segmented_sort(int key_type, int descending, void* d_keys,
 /* Batched sort of segments in HOST memory (keys, values and offsets on the
  * host; segment i is [h_offsets[i], h_offsets[i+1]) of h_keys): copies in,
  * sorts every segment, copies back, then synchronizes.  Consecutive segments
- * form about GBSORT_HOST_SPLIT_GROUPS (default 16) groups; a group's keys
+ * form groups of ~2^24 keys (2 to 16; GBSORT_HOST_SPLIT_GROUPS overrides);
+ * a group's keys
  * come in on one library-owned copy stream while the previous group sorts on
  * `stream` and the one before goes back on a second copy stream, so both
  * directions of the host link work at once (pinned memory for full speed).

@@ -143,7 +143,8 @@ def test_split_unusual_digits(gb, cuda, oracle, split_env, case):
 
 
 def test_split_at_default_threshold(gb, cuda, oracle):
-    """2^24 + 4097 u32 keys with index values: the split path as shipped."""
-    n = (1 << 24) + 4097
+    """2^25 + 4097 u32 keys with index values: the split path as shipped
+    (two groups)."""
+    n = (1 << 25) + 4097
     raw = raw_keys("u32", n, seed=11, dist=4)
     _host_sort_check(gb, cuda, oracle, "u32", raw, np.arange(n, dtype=np.uint32), desc=False)
