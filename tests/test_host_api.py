@@ -79,3 +79,19 @@ def test_double_buffer_rejects_bad_selector(gb):
         sel = ctypes.c_int(bad)
         assert f(2, 0, None, None, ctypes.byref(sel), ctypes.byref(tb), None, 10, None) == gb.ERR_INVALID_ARGUMENT
     assert f(2, 0, None, None, None, ctypes.byref(tb), None, 10, None) == gb.ERR_INVALID_ARGUMENT
+
+
+def test_segmented_host_buffer_bytes(gb):
+    """Host-memory batched sort: the keys and values once, plus one group's
+    workspace; malformed offsets give 0 (and no device work)."""
+    import numpy as np
+
+    rng = np.random.default_rng(4)
+    for kt, vb in (("u32", 4), ("u64", 0), ("u128", 16)):
+        sizes = np.exp2(rng.uniform(8, 20, 300)).astype(np.uint64)
+        off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+        n = int(off[-1])
+        hb = gb.segmented_host_buffer_bytes(kt, off, vb)
+        assert n * (KEY_BYTES[kt] + vb) < hb < 2 * n * (KEY_BYTES[kt] + vb)
+    assert gb.segmented_host_buffer_bytes("u32", np.array([0, 10, 5], dtype=np.uint64)) == 0
+    assert gb.segmented_host_buffer_bytes("u32", np.array([0], dtype=np.uint64)) > 0  # no segments
