@@ -751,6 +751,7 @@ def bench_batched(args, cfg, world, rank, local):
 
     hbm, peak_kind = peaks()
     algo_bytes = info["keys_in_cta"] * 2 * (4 + vb) + info["keys_in_onesweep"] * (4 + 4 * 2 * (4 + vb))
+    run_traffic, run_traffic_src = committed_traffic(args.config, n)
     mean_ms = total_ms / steps
     if rank != 0:
         return
@@ -773,9 +774,12 @@ def bench_batched(args, cfg, world, rank, local):
                                                 "the tile list) as one graph",
                      "algorithmic_bytes": algo_bytes,
                      "achieved": round(algo_bytes / (mean_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(algo_bytes / (mean_ms / 1e3) / 1e9 / hbm, 4), "traffic": None,
+                     "frac": round(algo_bytes / (mean_ms / 1e3) / 1e9 / hbm, 4), "traffic": run_traffic,
+                     "traffic_source": run_traffic_src,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "note": "CTA-sorted keys move 2*(K+V) bytes, onesweep keys K + P*2*(K+V); timed per replay"},
+                     "note": "CTA-sorted keys move 2*(K+V) bytes, onesweep keys K + P*2*(K+V); timed per replay; "
+                             "traffic: DRAM bytes of one run, from a smaller capture scaled by keys (a lower "
+                             "estimate: the smaller run keeps part of each pass in L2)"},
         "e2e": e2e,
         "cpu_baseline": cpu,
         "clocks": clk,

@@ -50,11 +50,11 @@ def test_committed_traffic_scales(bench):
         table = json.load(f)
     for config, e in table.items():
         assert os.path.exists(os.path.join(REPO, e["summary"])), e["summary"]
-        full = bench.CONFIGS[config]["n"]
+        full = bench.CONFIGS[config]["n"] or 508761137  # the batched run: keys of the benchmark's segments
         traffic, src = bench.committed_traffic(config, full)
         assert traffic == int(e["dram_bytes_per_launch"] * full / e["captured_n"])
         assert e["summary"] in src
-    assert bench.committed_traffic("c4", 1000) == (None, None)
+    assert bench.committed_traffic("c5", 1000) == (None, None)
 
 
 def test_step_stats(bench):
