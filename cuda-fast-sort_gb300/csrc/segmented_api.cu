@@ -71,21 +71,56 @@ std::mutex g_tune_mu;
 int g_tune[5][6][BUCKETS];
 bool g_tune_set[5][6];
 
-int path_for(int kb, int vb, uint64_t len, int s_max, int l_max) {
+// floor(log2 len), capped at the last bucket (0 for len 0)
+int size_bucket(uint64_t len) { return len ? std::min(BUCKETS - 1, 63 - __builtin_clzll(len)) : 0; }
+
+// The tuning-table row of one (key width, value size) and the CTA-sort
+// capacities, read once per plan (one lock, not one per segment).
+struct PathRule {
+    int table[BUCKETS];
+    bool set = false;
+    uint64_t s_max = 0, l_max = 0;
+};
+
+PathRule path_rule(int kb, int vb, int s_max, int l_max) {
+    PathRule r;
+    r.s_max = uint64_t(s_max);
+    r.l_max = uint64_t(l_max);
     const int wi = width_index(kb), vi = value_index(vb);
-    int bucket = 0;
-    while (bucket + 1 < BUCKETS && (uint64_t(1) << (bucket + 1)) <= len) ++bucket;
-    int path = -1;
-    {
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        if (g_tune_set[wi][vi]) path = g_tune[wi][vi][bucket];
-    }
-    if (path < 0) path = len <= uint64_t(s_max) ? GBSORT_PATH_CTA_S : len <= uint64_t(l_max) ? GBSORT_PATH_CTA_L
-                                                                                          : GBSORT_PATH_ONESWEEP;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    r.set = g_tune_set[wi][vi];
+    if (r.set) std::memcpy(r.table, g_tune[wi][vi], sizeof(r.table));
+    return r;
+}
+
+int path_of(const PathRule& r, uint64_t len) {
+    int path = r.set ? r.table[size_bucket(len)] : -1;
+    if (path < 0) path = len <= r.s_max ? GBSORT_PATH_CTA_S : len <= r.l_max ? GBSORT_PATH_CTA_L : GBSORT_PATH_ONESWEEP;
     // a path that cannot hold the segment falls through to the next one
-    if ((path == GBSORT_PATH_CTA_S || path == GBSORT_PATH_CTA_S4) && len > uint64_t(s_max)) path = GBSORT_PATH_CTA_L;
-    if (path == GBSORT_PATH_CTA_L && len > uint64_t(l_max)) path = GBSORT_PATH_ONESWEEP;
+    if ((path == GBSORT_PATH_CTA_S || path == GBSORT_PATH_CTA_S4) && len > r.s_max) path = GBSORT_PATH_CTA_L;
+    if (path == GBSORT_PATH_CTA_L && len > r.l_max) path = GBSORT_PATH_ONESWEEP;
     return path;
+}
+
+int path_for(int kb, int vb, uint64_t len, int s_max, int l_max) {
+    return path_of(path_rule(kb, vb, s_max, l_max), len);
+}
+
+// Largest first (for the balance of persistent CTAs pulling items in list
+// order): a stable counting sort by size bucket, linear in the items.
+void order_largest_first(std::vector<SegItem>& v) {
+    if (v.size() < 2) return;
+    size_t count[BUCKETS] = {};
+    for (const SegItem& it : v) ++count[size_bucket(it.end - it.begin)];
+    size_t start[BUCKETS];
+    size_t at = 0;
+    for (int b = BUCKETS - 1; b >= 0; --b) {
+        start[b] = at;
+        at += count[b];
+    }
+    std::vector<SegItem> out(v.size());
+    for (const SegItem& it : v) out[start[size_bucket(it.end - it.begin)]++] = it;
+    v.swap(out);
 }
 
 // One CTA (256 threads) per (segment, pass): exclusive scan of the segment's
@@ -189,10 +224,25 @@ int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t*
     }
     p->n_total = n_total;
     const uint64_t tile = uint64_t(p->pass.tile);
+    const PathRule rule = path_rule(p->kb, p->vb, p->cta_s.tile, p->cta_l.tile);
+    {  // size the onesweep lists once (their growth dominated planning)
+        uint64_t tiles = 0, items = 0, large = 0;
+        for (size_t s = 0; s < num; ++s) {
+            const uint64_t len = off[s + 1] - off[s];
+            if (len > 1 && path_of(rule, len) == GBSORT_PATH_ONESWEEP) {
+                tiles += (len + tile - 1) / tile;
+                items += (len + UPSWEEP_CHUNK - 1) / UPSWEEP_CHUNK;
+                ++large;
+            }
+        }
+        p->tiles.reserve(size_t(std::min<uint64_t>(tiles, 0xFFFFFFFFull)));
+        p->up_items.reserve(size_t(items));
+        p->large_begin.reserve(size_t(large));
+    }
     for (size_t s = 0; s < num; ++s) {
         const uint64_t b = off[s], e = off[s + 1], len = e - b;
         if (len <= 1) continue;  // already sorted
-        const int path = path_for(p->kb, p->vb, len, p->cta_s.tile, p->cta_l.tile);
+        const int path = path_of(rule, len);
         SegItem it{b, e, 0, 0};
         if (path == GBSORT_PATH_CTA_S) {
             p->small_s.push_back(it);
@@ -225,11 +275,10 @@ int build_plan(int key_type, size_t value_bytes, int descending, const uint64_t*
     }
     if (p->tiles.size() >= 0xFFFFFFFFull) return GBSORT_ERR_INVALID_ARGUMENT;
     // biggest segments first: better balance for the persistent CTA sorts
-    auto by_size = [](const SegItem& a, const SegItem& b) { return (a.end - a.begin) > (b.end - b.begin); };
-    std::stable_sort(p->small_s.begin(), p->small_s.end(), by_size);
-    std::stable_sort(p->small_l.begin(), p->small_l.end(), by_size);
-    std::stable_sort(p->small_s4.begin(), p->small_s4.end(), by_size);
-    std::stable_sort(p->up_items.begin(), p->up_items.end(), by_size);
+    order_largest_first(p->small_s);
+    order_largest_first(p->small_l);
+    order_largest_first(p->small_s4);
+    order_largest_first(p->up_items);
 
     const size_t L = p->large_begin.size();
     size_t o = 0;
