@@ -199,8 +199,10 @@ int gbsort_sort_keys_noalloc(int key_type, int descending, void* d_keys,
  * their top digit first and sorted in groups of consecutive buckets of
  * ~2^24 keys (2 to 16; GBSORT_HOST_SPLIT_GROUPS overrides), each copied
  * back on a library-owned copy stream while the next ones sort; the work is
- * ordered after what `stream` already holds.  Smaller arrays are copied in, sorted
- * and copied back on `stream`.  Either way the result is the in-place sort's. */
+ * ordered after what `stream` already holds.  Smaller arrays are copied in,
+ * sorted and copied back on `stream`.  Either way the result is the in-place
+ * sort's.  Calls from several threads are safe; their split-path copies share
+ * the copy stream and so run one after another. */
 size_t gbsort_host_buffer_bytes(int key_type, size_t value_bytes, size_t n);
 int gbsort_sort_host(int key_type, int descending, void* h_keys,
                      void* h_values, size_t value_bytes, size_t n,
@@ -277,7 +279,9 @@ int gbsort_segmented_sort(int key_type, int descending, void* d_keys,
  * `stream` and the one before goes back on a second copy stream, so both
  * directions of the host link work at once (pinned memory for full speed).
  * d_buffer (16-byte aligned) holds gbsort_segmented_host_buffer_bytes(...)
- * bytes: the keys and values once plus one group's workspace. */
+ * bytes: the keys and values once plus one group's workspace.  Calls from
+ * several threads are safe and run one at a time (they share the library's
+ * pinned staging of the groups' tables). */
 size_t gbsort_segmented_host_buffer_bytes(int key_type, size_t value_bytes,
                                           const uint64_t* h_offsets,
                                           size_t num_segments);
