@@ -144,11 +144,19 @@ def last_error() -> str:
 
 
 def _ptr(x) -> int | None:
+    """Address of a raw pointer (int), a torch tensor, or a C-contiguous
+    numpy array (host memory for the host-buffer sorts)."""
     if x is None:
         return None
     if isinstance(x, int):
         return x
-    return int(x.data_ptr())
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if hasattr(x, "ctypes") and hasattr(x, "flags"):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("numpy arrays passed as buffers must be C-contiguous")
+        return int(x.ctypes.data)
+    raise TypeError(f"cannot take the address of {type(x).__name__}")
 
 
 def _stream(s) -> int | None:

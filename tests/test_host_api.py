@@ -95,3 +95,19 @@ def test_segmented_host_buffer_bytes(gb):
         assert n * (KEY_BYTES[kt] + vb) < hb < 2 * n * (KEY_BYTES[kt] + vb)
     assert gb.segmented_host_buffer_bytes("u32", np.array([0, 10, 5], dtype=np.uint64)) == 0
     assert gb.segmented_host_buffer_bytes("u32", np.array([0], dtype=np.uint64)) > 0  # no segments
+
+
+def test_buffer_addresses(gb):
+    """Buffers may be raw addresses, torch tensors or contiguous numpy arrays."""
+    import numpy as np
+
+    a = np.zeros(16, np.uint32)
+    assert gb._ptr(a) == a.ctypes.data
+    assert gb._ptr(12345) == 12345 and gb._ptr(None) is None
+    with pytest.raises(ValueError):
+        gb._ptr(a[::2])
+    with pytest.raises(TypeError):
+        gb._ptr("not a buffer")
+    torch = pytest.importorskip("torch")
+    t = torch.zeros(4)
+    assert gb._ptr(t) == t.data_ptr()
