@@ -352,19 +352,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait on an mbarrier phase.  Returns false (after flagging the
-// workspace error word) if the limit ran out.
+// workspace error word) if the limit ran out.  The first probe does not
+// block; after it the limit is checked before every (potentially blocking)
+// try_wait, so a limit shorter than the copy always runs out.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns,
                                                   uint32_t* err) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_test_wait(bar, parity)) return true;
     const uint64_t t0 = global_timer_ns();
-    while (!mbar_try_wait(bar, parity)) {
+    for (;;) {
         if (global_timer_ns() - t0 > limit_ns) {
             atomicOr(err, ERRBIT_TIMEOUT);
             return false;
         }
+        if (mbar_try_wait(bar, parity)) return true;
     }
-    return true;
 }
 
 // Bounded wait for a status word of the current epoch.  On timeout, or when

@@ -189,6 +189,15 @@ GBSORT_DECLARE_TYPED(f128)
 int gbsort_sort_keys_noalloc(int key_type, int descending, void* d_keys,
                              size_t n, void* stream);
 
+/* Device-side status of the last gbsort_sort_keys_noalloc call of this
+ * (key_type, n): synchronizes `stream`, then reads the error word the sort's
+ * kernels left in the static scratch (GBSORT_OK, GBSORT_ERR_TIMEOUT when a
+ * bounded device wait ran out, GBSORT_ERR_INTERNAL for a failed bounds
+ * check).  Call it before the next noalloc call, which clears the word.  No
+ * counterpart in the reference (like the noalloc sort itself); allocates
+ * nothing. */
+int gbsort_noalloc_status(int key_type, size_t n, void* stream);
+
 /* Sort from HOST buffers: copies n keys (and values) from host memory into
  * the caller's device buffer d_buffer (16-byte aligned), sorts them there and
  * copies the result back, then synchronizes.  d_buffer must hold
