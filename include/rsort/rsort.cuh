@@ -11,7 +11,12 @@
 //     rsort::sort(d_keys, &temp_bytes, d_workspace, n);   // sort in place
 //
 // Entry points return void like rsort's; the status of the last call on this
-// thread is available from rsort::last_status() (0 = ok, see gbsort.h).
+// thread is available from rsort::last_status() (0 = ok, see gbsort.h).  That
+// status is what the host saw when the call returned (arguments, launches);
+// the sort itself runs later on the stream.  A failure on the device (a
+// bounded wait that ran out, a failed bounds check) is recorded in the
+// workspace: rsort::synchronize_status() waits for the last sort of this
+// thread, reads that record, folds it into last_status() and returns it.
 // Differences from rsort: the stream argument is honoured (rsort replaces it,
 // radix_kernel.cuh:583-601), n == 0 is a no-op, and any key type the
 // reference accepts maps onto one of gbsort's 13 key types by size and
@@ -71,43 +76,90 @@ inline int& last_status_ref() {
     return s;
 }
 
+// The last sort this thread enqueued (not a size query), for
+// synchronize_status().
+struct LastSort {
+    bool valid = false;
+    int key_type = 0;
+    size_t value_bytes = 0;
+    size_t n = 0;
+    void* workspace = nullptr;
+    cudaStream_t stream = nullptr;
+};
+inline LastSort& last_sort_ref() {
+    static thread_local LastSort s;
+    return s;
+}
+
+inline void record(int status, int key_type, size_t value_bytes, uint8_t* d_workspace, size_t n,
+                   cudaStream_t stream) {
+    last_status_ref() = status;
+    LastSort& l = last_sort_ref();
+    l.valid = status == GBSORT_OK && d_workspace != nullptr && n != 0;
+    l.key_type = key_type;
+    l.value_bytes = value_bytes;
+    l.n = n;
+    l.workspace = d_workspace;
+    l.stream = stream;
+}
+
 }  // namespace detail
 
-// Status of the last rsort call on this thread (GBSORT_OK == 0).
+// Status of the last rsort call on this thread (GBSORT_OK == 0), as the host
+// saw it when the call returned.
 inline int last_status() { return detail::last_status_ref(); }
+
+// Waits for the last sort this thread enqueued (its stream), then reports
+// what happened on the device: GBSORT_OK, or GBSORT_ERR_TIMEOUT /
+// GBSORT_ERR_INTERNAL recorded by the kernels.  The result also becomes
+// last_status().  Read it before the workspace is reused: the next sort on
+// the same workspace clears the record.
+inline int synchronize_status() {
+    detail::LastSort& l = detail::last_sort_ref();
+    if (!l.valid) return detail::last_status_ref();
+    const int st = gbsort_workspace_status(l.key_type, l.value_bytes, l.n, l.workspace, l.stream);
+    detail::last_status_ref() = st;
+    return st;
+}
 
 template <typename Key_T, typename Len_T>
 inline void sort(Key_T* d_inout, size_t* temp_bytes, uint8_t* d_workspace, Len_T n,
                  cudaStream_t capture_stream = nullptr) {
     static_assert(std::is_integral<Len_T>::value, "Type of N (Len_T) must be an integral type");
-    detail::last_status_ref() = gbsort_sort_keys(detail::key_type_id<Key_T>(), 0, d_inout, temp_bytes, d_workspace,
-                                                 static_cast<size_t>(n), capture_stream);
+    const int kt = detail::key_type_id<Key_T>();
+    detail::record(gbsort_sort_keys(kt, 0, d_inout, temp_bytes, d_workspace, static_cast<size_t>(n), capture_stream),
+                   kt, 0, d_workspace, static_cast<size_t>(n), capture_stream);
 }
 
 template <typename Key_T, typename Len_T>
 inline void sort_descending(Key_T* d_inout, size_t* temp_bytes, uint8_t* d_workspace, Len_T n,
                             cudaStream_t capture_stream = nullptr) {
     static_assert(std::is_integral<Len_T>::value, "Type of N (Len_T) must be an integral type");
-    detail::last_status_ref() = gbsort_sort_keys(detail::key_type_id<Key_T>(), 1, d_inout, temp_bytes, d_workspace,
-                                                 static_cast<size_t>(n), capture_stream);
+    const int kt = detail::key_type_id<Key_T>();
+    detail::record(gbsort_sort_keys(kt, 1, d_inout, temp_bytes, d_workspace, static_cast<size_t>(n), capture_stream),
+                   kt, 0, d_workspace, static_cast<size_t>(n), capture_stream);
 }
 
 template <typename Key_T, typename Len_T, typename Value_T>
 inline void sort_pairs(Key_T* d_inout, Value_T* d_inout_values, size_t* temp_bytes, uint8_t* d_workspace, Len_T n,
                        cudaStream_t capture_stream = nullptr) {
     static_assert(std::is_integral<Len_T>::value, "Type of N (Len_T) must be an integral type");
-    detail::last_status_ref() =
-        gbsort_sort_pairs(detail::key_type_id<Key_T>(), 0, d_inout, d_inout_values, detail::value_bytes<Value_T>(),
-                          temp_bytes, d_workspace, static_cast<size_t>(n), capture_stream);
+    const int kt = detail::key_type_id<Key_T>();
+    constexpr size_t vb = detail::value_bytes<Value_T>();
+    detail::record(gbsort_sort_pairs(kt, 0, d_inout, d_inout_values, vb, temp_bytes, d_workspace,
+                                     static_cast<size_t>(n), capture_stream),
+                   kt, vb, d_workspace, static_cast<size_t>(n), capture_stream);
 }
 
 template <typename Key_T, typename Len_T, typename Value_T>
 inline void sort_pairs_descending(Key_T* d_inout, Value_T* d_inout_values, size_t* temp_bytes, uint8_t* d_workspace,
                                   Len_T n, cudaStream_t capture_stream = nullptr) {
     static_assert(std::is_integral<Len_T>::value, "Type of N (Len_T) must be an integral type");
-    detail::last_status_ref() =
-        gbsort_sort_pairs(detail::key_type_id<Key_T>(), 1, d_inout, d_inout_values, detail::value_bytes<Value_T>(),
-                          temp_bytes, d_workspace, static_cast<size_t>(n), capture_stream);
+    const int kt = detail::key_type_id<Key_T>();
+    constexpr size_t vb = detail::value_bytes<Value_T>();
+    detail::record(gbsort_sort_pairs(kt, 1, d_inout, d_inout_values, vb, temp_bytes, d_workspace,
+                                     static_cast<size_t>(n), capture_stream),
+                   kt, vb, d_workspace, static_cast<size_t>(n), capture_stream);
 }
 
 }  // namespace rsort

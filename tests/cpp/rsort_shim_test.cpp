@@ -137,6 +137,46 @@ bool run_keys_case(const char* name, size_t n) {
     return ok;
 }
 
+// A sort whose bounded device waits run out (a 1 ns limit) returns normally
+// from the host call; rsort::synchronize_status() reports the timeout the
+// kernels recorded in the workspace.  The same workspace then sorts
+// correctly again and reports OK.
+bool run_timeout_case() {
+    const size_t n = size_t(1) << 21;
+    std::vector<uint32_t> keys(n);
+    for (auto& k : keys) k = uint32_t(rng());
+    uint32_t* d = nullptr;
+    cudaMalloc(&d, n * sizeof(uint32_t));
+    size_t temp_bytes = 0;
+    uint8_t* ws = nullptr;
+    rsort::sort(d, &temp_bytes, ws, n);
+    cudaMalloc(&ws, temp_bytes);
+    const uint64_t old_limit = gbsort_get_wait_limit_ns();
+    gbsort_set_wait_limit_ns(1);
+    int host_st = -1, dev_st = GBSORT_OK;
+    for (int attempt = 0; attempt < 3 && dev_st == GBSORT_OK; ++attempt) {
+        cudaMemcpy(d, keys.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        rsort::sort(d, &temp_bytes, ws, n);
+        host_st = rsort::last_status();
+        dev_st = rsort::synchronize_status();
+    }
+    const bool folded = rsort::last_status() == dev_st;
+    gbsort_set_wait_limit_ns(old_limit);
+    cudaMemcpy(d, keys.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    rsort::sort(d, &temp_bytes, ws, n);
+    const int ok_st = rsort::synchronize_status();
+    std::vector<uint32_t> out(n);
+    cudaMemcpy(out.data(), d, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    cudaFree(ws);
+    std::sort(keys.begin(), keys.end());
+    const bool ok = host_st == GBSORT_OK && dev_st == GBSORT_ERR_TIMEOUT && folded && ok_st == GBSORT_OK &&
+                    out == keys;
+    std::printf("%-26s n=%-8zu host %d, device %d, after %d  %s\n", "timeout via shim", n, host_st, dev_st, ok_st,
+                ok ? "passed" : "FAILED");
+    return ok;
+}
+
 }  // namespace
 
 int main() {
@@ -154,6 +194,7 @@ int main() {
     uint32_t* none = nullptr;
     rsort::sort(none, &tb, reinterpret_cast<uint8_t*>(1), size_t(0));
     ok &= rsort::last_status() == 0;
+    ok &= run_timeout_case();
     std::printf("%s\n", ok ? "ALL PASSED" : "SOME FAILED");
     return ok ? 0 : 1;
 }
