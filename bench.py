@@ -3,8 +3,8 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W]
                     [--config c2b|c1|c2a|c3a|c3b|c4|c5] [--impl gbsort|reference]
-                    [--n N] [--rate R] [--e2e-steps S] [--cpu-seconds T]
-                    [--no-cpu-baseline] [--no-cub]
+                    [--n N] [--segments S] [--rate R] [--e2e-steps S]
+                    [--cpu-seconds T] [--no-cpu-baseline] [--no-cub] [--headline-only]
 
 One step = one sort (histogram upsweep + one onesweep pass per key byte) of a
 fresh batch of synthetic keys already resident in HBM.  Before each step the
@@ -37,6 +37,12 @@ Extra keys on the JSON line:
   cpu_baseline  the CPU oracle (std::stable_sort of twiddled keys, 1 thread)
                 on a bounded sample of the same workload (rank 0, N=1 only)
   clocks        nvidia-smi samples taken during the timed region
+The default run (c2b, one GPU) adds the rest of the benchmark metric after
+the headline, each measured the way its own --config run measures it (fewer
+steps, no CPU baseline): `plain_configs` (c1, c2a, c3a, c3b: value, roofline,
+CUB on the same GPU, e2e), `batched` (c4: value, speedup_vs_loop, roofline,
+e2e) and `serving` (c5: capacity, p50/p99 latency at 70 % load,
+identical_alone_and_in_mix).  --headline-only skips them.
 --impl reference times the reference path's CPU implementation (the oracle
 port: parallel stable sort on every host core) on samples of the workload.
 """
@@ -543,7 +549,7 @@ def bench_gbsort(args, cfg, world, rank, local):
                          f"{len(times)} reps ({sum(times):.1f} s)"}
 
     if rank != 0:
-        return
+        return None
     plan = gbsort.plan(kt, n, vb)
     line = {
         "metric": PLAIN_METRIC, "value": round(value, 3),
@@ -572,7 +578,7 @@ def bench_gbsort(args, cfg, world, rank, local):
                              "the pass-skip fix-up copy (exits at once when no pass was skipped); plus one memset",
         "sorted_check": ok,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def bench_batched(args, cfg, world, rank, local):
@@ -754,7 +760,7 @@ def bench_batched(args, cfg, world, rank, local):
     run_traffic, run_traffic_src = committed_traffic(args.config, n)
     mean_ms = total_ms / steps
     if rank != 0:
-        return
+        return None
     line = {
         "metric": BATCHED_METRIC, "value": round(value, 3), "unit": "Gkeys/s",
         "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
@@ -788,7 +794,7 @@ def bench_batched(args, cfg, world, rank, local):
         "gpu_launches": steps * (info["kernel_launches"] + 2),
         "gpu_launches_note": "per step: the batched run's kernels plus two input-generation kernels",
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def bench_serving(args, cfg, world, rank, local):
@@ -981,7 +987,7 @@ def bench_serving(args, cfg, world, rank, local):
                "sample": f"{count} requests of the same distribution ({done_keys} keys), std::stable_sort of "
                          f"twiddled keys, 1 thread, sorting only (no copies)"}
     if rank != 0:
-        return
+        return None
     mean_keys = keys_cap / n_cap
     hbm, _ = peaks()
     line = {
@@ -1034,7 +1040,90 @@ def bench_serving(args, cfg, world, rank, local):
         "gpu_launches": cap_stats["kernel_launches"],
         "identical_alone_and_in_mix": identical, "checked_requests": len(checks), "failed_requests": len(bad),
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def _sub_args(args, config, steps):
+    """Arguments of a companion run: few steps, no CPU baseline (the headline
+    line carries it), short e2e."""
+    import copy
+
+    sub = copy.copy(args)
+    sub.config = config
+    sub.steps = steps
+    sub.warmup = 3
+    sub.no_cpu_baseline = True
+    sub.e2e_steps = min(args.e2e_steps, 2)
+    sub.n = 0
+    sub.rate = 0.0
+    sub.segments = 0
+    return sub
+
+
+def _release_device_memory():
+    import gc
+
+    import torch
+
+    gc.collect()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
+def companion_runs(args, local) -> dict:
+    """The rest of the benchmark metric beside the 2^28 u32 headline, on the
+    same GPU after it: the other plain configurations (c1, c2a, c3a, c3b),
+    the batched sort of 4096 segments against looping the plain sort (c4) and
+    the sort server's capacity and p50/p99 latency at load (c5).  Each is the
+    same measurement as its own --config run, with fewer steps."""
+    out = {}
+    plain = {}
+    for c, steps in (("c1", 50), ("c2a", 10), ("c3a", 8), ("c3b", 8)):
+        t0 = time.time()
+        try:
+            ln = bench_gbsort(_sub_args(args, c, steps), CONFIGS[c], 1, 0, local)
+            plain[c] = {
+                "workload": ln["config"]["workload"], "value": ln["value"], "unit": ln["unit"],
+                "ms_per_step": ln["ms_per_step"], "steps": ln["steps"], "vs_baseline": ln["vs_baseline"],
+                "baseline_published": ln["baseline_published"],
+                "roofline": {k: ln["roofline"][k] for k in ("kernel", "achieved", "peak", "unit", "frac",
+                                                            "mean_launch_ms", "algorithmic_bytes_per_launch")},
+                "sort_roofline": ln["sort_roofline"], "passes": ln["config"]["passes"],
+                "e2e": ln["e2e"], "cub": (ln["comparators"]["cub"] or {}).get("value"),
+                "sorted_check": ln["sorted_check"], "clocks": ln["clocks"],
+                "seconds": round(time.time() - t0, 1)}
+        except Exception as e:  # one companion failing does not void the headline
+            plain[c] = {"error": f"{type(e).__name__}: {e}"}
+        _release_device_memory()
+    out["plain_configs"] = plain
+    t0 = time.time()
+    try:
+        ln = bench_batched(_sub_args(args, "c4", 10), CONFIGS["c4"], 1, 0, local)
+        out["batched"] = {
+            "metric": ln["metric"], "workload": ln["config"]["workload"], "value": ln["value"], "unit": ln["unit"],
+            "ms_per_step": ln["ms_per_step"], "steps": ln["steps"], "n_keys": ln["config"]["n_keys"],
+            "segments": ln["config"]["segments"], "speedup_vs_loop": ln["speedup_vs_loop"],
+            "loop_baseline": ln["loop_baseline"], "roofline": ln["roofline"], "e2e": ln["e2e"],
+            "paths": ln["config"]["paths"], "sorted_check": ln["sorted_check"], "clocks": ln["clocks"],
+            "gpu_launches": ln["gpu_launches"], "seconds": round(time.time() - t0, 1)}
+    except Exception as e:
+        out["batched"] = {"error": f"{type(e).__name__}: {e}"}
+    _release_device_memory()
+    t0 = time.time()
+    try:
+        ln = bench_serving(_sub_args(args, "c5", 20), CONFIGS["c5"], 1, 0, local)
+        out["serving"] = {
+            "metric": ln["metric"], "workload": ln["config"]["workload"], "value": ln["value"], "unit": ln["unit"],
+            "requests_capacity_phase": ln["config"]["requests_capacity_phase"],
+            "requests_load_phase": ln["config"]["requests_load_phase"], "capacity": ln["capacity"],
+            "latency": ln["latency"], "identical_alone_and_in_mix": ln["identical_alone_and_in_mix"],
+            "checked_requests": ln["checked_requests"], "failed_requests": ln["failed_requests"],
+            "roofline": ln["roofline"], "link_roofline": ln["link_roofline"], "e2e": ln["e2e"],
+            "clocks": ln["clocks"], "gpu_launches": ln["gpu_launches"], "seconds": round(time.time() - t0, 1)}
+    except Exception as e:
+        out["serving"] = {"error": f"{type(e).__name__}: {e}"}
+    _release_device_memory()
+    return out
 
 
 def main():
@@ -1050,22 +1139,36 @@ def main():
     ap.add_argument("--no-cub", action="store_true", help="skip the CUB comparator")
     ap.add_argument("--n", type=int, default=0,
                     help="override the configuration's key count (a smaller case for profiling)")
+    ap.add_argument("--segments", type=int, default=0,
+                    help="c4: override the number of segments (a smaller batch for profiling)")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="c5: Poisson arrival rate in requests/s (0: the configured fraction of measured capacity)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="c2b: skip the companion runs (other plain configurations, batched, serving)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # timing rule: at least 3 warm-up steps
     world, rank, local = dist_init()
     cfg = CONFIGS[args.config]
     if args.n > 0 and cfg["n"]:
         cfg = dict(cfg, n=args.n, workload=cfg["workload"] + f" (n overridden to {args.n})")
+    if args.segments > 0 and "segments" in cfg:
+        cfg = dict(cfg, segments=args.segments, workload=cfg["workload"] + f" (segments overridden to {args.segments})")
     if args.impl == "reference":
         bench_reference(args, cfg, world, rank)
-    elif cfg.get("serving"):
-        bench_serving(args, cfg, world, rank, local)
-    elif "segments" in cfg:
-        bench_batched(args, cfg, world, rank, local)
     else:
-        bench_gbsort(args, cfg, world, rank, local)
+        if cfg.get("serving"):
+            line = bench_serving(args, cfg, world, rank, local)
+        elif "segments" in cfg:
+            line = bench_batched(args, cfg, world, rank, local)
+        else:
+            line = bench_gbsort(args, cfg, world, rank, local)
+        if line is not None and args.config == "c2b" and args.n == 0 and world == 1 and not args.headline_only:
+            _release_device_memory()
+            t0 = time.time()
+            line.update(companion_runs(args, local))
+            line["companion_seconds"] = round(time.time() - t0, 1)
+        if line is not None:
+            print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 

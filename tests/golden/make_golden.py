@@ -1,8 +1,9 @@
 """Generates tests/golden/ fixtures by running the reference's own code.
 
-Run in a container that has the reference sources (default /root/reference):
+Run where a checkout of the reference sources exists:
 
-    python tests/golden/make_golden.py [--reference DIR]
+    python tests/golden/make_golden.py --reference DIR
+    (or RSORT_REFERENCE_DIR=DIR python tests/golden/make_golden.py)
 
 It builds oracle/_ref/ref_probe (oracle/Makefile target ``ref``), which
 compiles the reference's include/rsort/detail/tuning.cuh + utils.cuh on the
@@ -61,8 +62,11 @@ def random_values(width: int, count: int, seed: int) -> list[int]:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("RSORT_REFERENCE_DIR", ""),
+                    help="checkout of the reference rsort (default: $RSORT_REFERENCE_DIR)")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("name the reference checkout with --reference or RSORT_REFERENCE_DIR")
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref",
                     f"REFERENCE={args.reference}"], check=True)
     probe = os.path.join(REPO, "oracle", "_ref", "ref_probe")
