@@ -215,6 +215,12 @@ __device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ uint64_t global_timer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -312,6 +318,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -379,6 +389,37 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
         }
         if (mbar_try_wait(bar, parity)) return true;
     }
+}
+
+// Grid-wide barrier of a cooperative launch (every CTA resident at once).
+// `counter` starts at 0; the k-th barrier of the launch (k = 1, 2, ...) waits
+// until it reaches k * gridDim.x.  Thread 0 of each CTA arrives with a
+// release and waits with acquire loads, bounded by limit_ns: a wait that runs
+// out records ERRBIT_TIMEOUT and the barrier returns false on every thread
+// of that CTA, so the caller can leave instead of hanging.
+__device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t k, uint64_t limit_ns, uint32_t* err) {
+    __syncthreads();
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        const uint32_t target = k * gridDim.x;
+        __threadfence();
+        atomicAdd(counter, 1u);
+        if (ld_acquire(counter) < target) {
+            const uint64_t t0 = global_timer_ns();
+            uint32_t sleep_ns = 32;
+            while (ld_acquire(counter) < target) {
+                if (global_timer_ns() - t0 > limit_ns) {
+                    atomicOr(err, ERRBIT_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(sleep_ns);
+                if (sleep_ns < 256) sleep_ns <<= 1;
+            }
+        }
+        __threadfence();
+    }
+    return __syncthreads_and(ok) != 0;
 }
 
 // Bounded wait for a status word of the current epoch.  On timeout, or when

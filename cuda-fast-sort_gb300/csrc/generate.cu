@@ -1,5 +1,6 @@
 // generate.cu — seeded synthetic inputs on the device (gbsort_generate) and
-// the bounded-wait probe (gbsort_probe_wait_timeout).
+// the bounded-wait probes (gbsort_probe_wait_timeout,
+// gbsort_probe_barrier_timeout).
 //
 // The integer streams match cuda-fast-sort_gb300/gbsort/gen.py bit for bit.
 // Distributions 4/5 restate the reference's init_keys kernel
@@ -118,6 +119,14 @@ __global__ void probe_wait_kernel(uint32_t* scratch, uint64_t limit_ns) {
     (void)wait_status<Codec>(word, 1u, limit_ns, err);
 }
 
+// One grid barrier that can never complete: a single CTA waits for a second
+// arrival (phase 2 of a one-CTA grid) that nothing makes.
+__global__ void probe_barrier_kernel(uint32_t* scratch, uint64_t limit_ns) {
+    uint32_t* counter = scratch;
+    uint32_t* err = scratch + 1;
+    (void)grid_barrier(counter, 2u, limit_ns, err);
+}
+
 }  // namespace
 }  // namespace gbsort
 
@@ -158,6 +167,26 @@ int gbsort_probe_wait_timeout(void* d_scratch, uint64_t limit_ns, void* stream) 
     if (e == cudaSuccess) e = cudaMemcpy(&err, static_cast<uint32_t*>(d_scratch) + 1, 4, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
         set_last_error("wait probe", e);
+        return GBSORT_ERR_CUDA;
+    }
+    return err ? GBSORT_ERR_TIMEOUT : GBSORT_OK;
+}
+
+int gbsort_probe_barrier_timeout(void* d_scratch, uint64_t limit_ns, void* stream) {
+    using namespace gbsort;
+    if (d_scratch == nullptr) return GBSORT_ERR_INVALID_ARGUMENT;
+    if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemsetAsync(d_scratch, 0, 64, s);
+    if (e == cudaSuccess) {
+        probe_barrier_kernel<<<1, 64, 0, s>>>(static_cast<uint32_t*>(d_scratch), limit_ns);
+        e = cudaGetLastError();
+    }
+    uint32_t err = 0;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpy(&err, static_cast<uint32_t*>(d_scratch) + 1, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_last_error("barrier probe", e);
         return GBSORT_ERR_CUDA;
     }
     return err ? GBSORT_ERR_TIMEOUT : GBSORT_OK;

@@ -3,6 +3,7 @@
 // parallel translation units.
 #pragma once
 
+#include "fused_short.cuh"
 #include "onesweep.cuh"
 #include "segmented.cuh"
 #include "shapes.h"
@@ -40,6 +41,18 @@ const KernelEntry* pass_entries_for() {
         {r4.e[0], r4.e[1], r4.e[2]},    {r8.e[0], r8.e[1], r8.e[2]},    {r16.e[0], r16.e[1], r16.e[2]},
     };
     return &e[0][0];
+}
+
+// The one-launch sort of short keys-only arrays, in the short-array pass shape.
+template <int KB>
+const KernelEntry* fused_entry_for() {
+    using S = PassShapeSmall<KB, 0>;
+    using G = PassGeom<KB, 0, S::THREADS, S::IPT>;
+    static const KernelEntry e = {
+        reinterpret_cast<const void*>(
+            &fused_short_kernel<KB, uint32_t, S::THREADS, S::IPT, S::MIN_CTAS, S::LOOKBACK_WINDOW>),
+        S::THREADS, S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
+    return &e;
 }
 
 template <int KB>

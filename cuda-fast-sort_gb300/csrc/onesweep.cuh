@@ -196,15 +196,18 @@ struct PassGeom {
 // count), each segment's first tile publishes an inclusive prefix of its own
 // so lookback chains never cross segments, and digit bases come per segment
 // from p.seg_gofs.
-template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int MIN_CTAS, int LBW>
-__global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassParams p) {
+// The pass as a device function: the pass kernel below runs it once; the
+// one-launch short sort (fused_short.cuh) runs it once per digit pass with a
+// grid barrier in between.  REUSE: the CTA runs further passes after this
+// one, so the mbarriers are invalidated on the way out (a clean exit, or one
+// that drained its copies after an error) and initialised again next time.
+template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int LBW, bool REUSE = false>
+__device__ __forceinline__ void onesweep_pass_body(const PassParams& p, uint8_t* smem) {
     using U = typename KeyBits<KB>::U;
     using V = typename ValBits<VB>::V;
     using G = PassGeom<KB, VB, THREADS, IPT>;
     using Codec = StatusCodec<W, KB>;
     constexpr bool PAIRS = VB > 0;
-
-    extern __shared__ __align__(128) uint8_t smem[];
     uint32_t* whist = reinterpret_cast<uint32_t*>(smem + G::HIST_OFF);
     unsigned long long* gexcl = reinterpret_cast<unsigned long long*>(smem + G::GEXCL_OFF);
     unsigned long long* binb = reinterpret_cast<unsigned long long*>(smem + G::BINB_OFF);
@@ -497,6 +500,11 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
                 mbar_wait_bounded(&mbar[b], ((parity >> b) & 1u) ^ 1u, DRAIN_LIMIT_NS, p.err);
                 if (next_issued) mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
                 if constexpr (G::LATE) mbar_wait_bounded(&mbar[2], vparity, DRAIN_LIMIT_NS, p.err);
+                if constexpr (REUSE) {
+                    mbar_inval(&mbar[0]);
+                    mbar_inval(&mbar[1]);
+                    mbar_inval(&mbar[2]);
+                }
             }
             return;
         }
@@ -683,6 +691,11 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
                     mbar_wait_bounded(&mbar[2], vparity ^ 1u, DRAIN_LIMIT_NS, p.err);
                     if (next_issued)
                         mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
+                    if constexpr (REUSE) {
+                        mbar_inval(&mbar[0]);
+                        mbar_inval(&mbar[1]);
+                        mbar_inval(&mbar[2]);
+                    }
                 }
                 return;
             }
@@ -692,6 +705,61 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassPa
         cur = next_info;
         ++it;
     }
+    if constexpr (REUSE) {
+        __syncthreads();  // no thread still waits on a barrier
+        if (tid == 0) {
+            mbar_inval(&mbar[0]);
+            mbar_inval(&mbar[1]);
+            mbar_inval(&mbar[2]);
+        }
+    }
+}
+
+template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int MIN_CTAS, int LBW>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS) onesweep_pass_kernel(PassParams p) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    onesweep_pass_body<KB, VB, W, THREADS, IPT, SEG, LBW>(p, smem);
+}
+
+// Copies `bytes` from src to dst with all threads of the grid (16-byte
+// vectors when both ends allow, else 4-byte words, else bytes).
+__device__ __forceinline__ void grid_copy_bytes(void* dst, const void* src, uint64_t bytes) {
+    const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
+    uint64_t done = 0;
+    if ((a & 15u) == 0) {
+        const uint64_t v = bytes / 16;
+        for (uint64_t i = t; i < v; i += stride) static_cast<uint4*>(dst)[i] = static_cast<const uint4*>(src)[i];
+        done = v * 16;
+    } else if ((a & 3u) == 0) {
+        const uint64_t v = bytes / 4;
+        for (uint64_t i = t; i < v; i += stride)
+            static_cast<uint32_t*>(dst)[i] = static_cast<const uint32_t*>(src)[i];
+        done = v * 4;
+    }
+    for (uint64_t i = done + t; i < bytes; i += stride)
+        static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
+}
+
+// After uniform-pass skipping: the executed passes' parity left the result
+// in the other buffer than the one it belongs in (in place: an odd count
+// left it in the alternate buffer); copy it across.  Otherwise nothing to do.
+__device__ __forceinline__ void fixup_body(const FixupParams& f) {
+    // the executed pass kernels left their count; none ran when the word is 0
+    const uint32_t w = *f.executed;
+    const int executed = (w >> 31) ? int(w & 0xFFu) : 0;
+    if (f.copy_keys_in) {  // input-preserving: only when no pass wrote the output
+        if (executed != 0) return;
+        grid_copy_bytes(f.keys_a, f.copy_keys_in, f.key_bytes_total);
+        if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.copy_vals_in, f.val_bytes_total);
+        return;
+    }
+    if ((executed & 1) == f.want_odd) return;
+    // the result sits in b after an odd number of executed passes, else in a
+    const bool in_b = (executed & 1) != 0;
+    grid_copy_bytes(in_b ? f.keys_a : f.keys_b, in_b ? f.keys_b : f.keys_a, f.key_bytes_total);
+    if (f.val_bytes_total) grid_copy_bytes(in_b ? f.vals_a : f.vals_b, in_b ? f.vals_b : f.vals_a, f.val_bytes_total);
 }
 
 }  // namespace gbsort

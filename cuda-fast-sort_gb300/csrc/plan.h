@@ -14,7 +14,7 @@ namespace gbsort {
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Control block at the start of the workspace's control region:
-//   [gp_counts: passes*256 u64][tile_counters: 16 u32][err: u32][executed: u32][pad]
+//   [gp_counts: passes*256 u64][tile_counters: 16 u32][err: u32][executed: u32][barrier: u32][pad]
 // executed: written by the pass kernels that run (bit 31 | passes executed)
 // when uniform passes are skipped; 0 when none ran.
 struct CtlLayout {
@@ -22,6 +22,7 @@ struct CtlLayout {
     size_t counters_off = 0;
     size_t err_off = 0;
     size_t exec_off = 0;
+    size_t barrier_off = 0;  // grid barrier counter of the one-launch short sort
     size_t bytes = 0;
     static CtlLayout make(int passes) {
         CtlLayout c;
@@ -29,7 +30,8 @@ struct CtlLayout {
         c.counters_off = size_t(passes) * 256 * 8;
         c.err_off = c.counters_off + 16 * 4;
         c.exec_off = c.err_off + 4;
-        c.bytes = align_up(c.exec_off + 4, 256);
+        c.barrier_off = c.exec_off + 4;
+        c.bytes = align_up(c.barrier_off + 4, 256);
         return c;
     }
 };
@@ -43,6 +45,9 @@ struct Plan {
     bool wide_status = false;
     KernelEntry pass{};
     KernelEntry upsweep{};
+    // One-launch path (short keys-only arrays): upsweep, passes and fix-up in
+    // one cooperative kernel of pass's shape.  fused.fn == nullptr: not used.
+    KernelEntry fused{};
     uint64_t n = 0;
     uint32_t num_tiles = 0;
     // workspace layout (offsets from the workspace base)

@@ -82,12 +82,15 @@ struct PassShape {
 // sweeps: -DGBSORT_SHAPE_KB=.. -DGBSORT_SHAPE_VB=.. -DGBSORT_SHAPE_THREADS=..
 // -DGBSORT_SHAPE_IPT=.. -DGBSORT_SHAPE_MIN_CTAS=..
 #if defined(GBSORT_SHAPE_KB)
+#ifndef GBSORT_SHAPE_WINDOW
+#define GBSORT_SHAPE_WINDOW 4
+#endif
 template <>
 struct PassShape<GBSORT_SHAPE_KB, GBSORT_SHAPE_VB> {
     static constexpr int THREADS = GBSORT_SHAPE_THREADS;
     static constexpr int IPT = GBSORT_SHAPE_IPT;
     static constexpr int MIN_CTAS = GBSORT_SHAPE_MIN_CTAS;
-    static constexpr int LOOKBACK_WINDOW = 4;
+    static constexpr int LOOKBACK_WINDOW = GBSORT_SHAPE_WINDOW;
 };
 #endif
 

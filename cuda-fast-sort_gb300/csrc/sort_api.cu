@@ -24,6 +24,7 @@
 #include "gbsort.h"
 #include "plan.h"
 #include "device_common.cuh"
+#include "onesweep.cuh"
 #include "sort_params.h"
 
 namespace gbsort {
@@ -38,6 +39,22 @@ const KernelEntry* upsweep_entry_k2();
 const KernelEntry* upsweep_entry_k4();
 const KernelEntry* upsweep_entry_k8();
 const KernelEntry* upsweep_entry_k16();
+const KernelEntry* fused_entry_k1();
+const KernelEntry* fused_entry_k2();
+const KernelEntry* fused_entry_k4();
+const KernelEntry* fused_entry_k8();
+const KernelEntry* fused_entry_k16();
+
+const KernelEntry* fused_entry(int kb) {
+    switch (kb) {
+        case 1: return fused_entry_k1();
+        case 2: return fused_entry_k2();
+        case 4: return fused_entry_k4();
+        case 8: return fused_entry_k8();
+        case 16: return fused_entry_k16();
+        default: return nullptr;
+    }
+}
 
 const KernelEntry* pass_entries(int kb) {
     switch (kb) {
@@ -64,52 +81,23 @@ const KernelEntry* upsweep_entry(int kb) {
 namespace {
 
 std::atomic<uint64_t> g_wait_limit_ns{2000000000ull};
+// One-launch sort of short keys-only arrays: off unless GBSORT_SHORT_FUSED=1
+// or switched on (gbsort_set_short_fused).
+std::atomic<int> g_short_fused{[] {
+    const char* v = std::getenv("GBSORT_SHORT_FUSED");
+    return (v && v[0] == '1') ? 1 : 0;
+}()};
 // Uniform-digit pass skipping: on unless GBSORT_PASS_SKIP=0 or switched off.
 std::atomic<int> g_pass_skip{[] {
     const char* v = std::getenv("GBSORT_PASS_SKIP");
     return (v && v[0] == '0') ? 0 : 1;
 }()};
 
-// Copies `bytes` from src to dst with all threads of the grid (16-byte
-// vectors when both ends allow, else 4-byte words, else bytes).
-__device__ void grid_copy_bytes(void* dst, const void* src, uint64_t bytes) {
-    const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
-    uint64_t done = 0;
-    if ((a & 15u) == 0) {
-        const uint64_t v = bytes / 16;
-        for (uint64_t i = t; i < v; i += stride) static_cast<uint4*>(dst)[i] = static_cast<const uint4*>(src)[i];
-        done = v * 16;
-    } else if ((a & 3u) == 0) {
-        const uint64_t v = bytes / 4;
-        for (uint64_t i = t; i < v; i += stride)
-            static_cast<uint32_t*>(dst)[i] = static_cast<const uint32_t*>(src)[i];
-        done = v * 4;
-    }
-    for (uint64_t i = done + t; i < bytes; i += stride)
-        static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
-}
-
-// After uniform-pass skipping: the executed passes' parity left the result
-// in the other buffer than the one it belongs in (in place: an odd count
-// left it in the alternate buffer); copy it across.  Otherwise nothing to do.
+// After uniform-pass skipping, copies the result home when the executed
+// passes' parity left it in the other buffer (fixup_body).
 __global__ void __launch_bounds__(256) skip_fixup_kernel(FixupParams f) {
     grid_dependency_wait();  // launched as a dependent of the last pass
-    // the executed pass kernels left their count; none ran when the word is 0
-    const uint32_t w = *f.executed;
-    const int executed = (w >> 31) ? int(w & 0xFFu) : 0;
-    if (f.copy_keys_in) {  // input-preserving: only when no pass wrote the output
-        if (executed != 0) return;
-        grid_copy_bytes(f.keys_a, f.copy_keys_in, f.key_bytes_total);
-        if (f.val_bytes_total) grid_copy_bytes(f.vals_a, f.copy_vals_in, f.val_bytes_total);
-        return;
-    }
-    if ((executed & 1) == f.want_odd) return;
-    // the result sits in b after an odd number of executed passes, else in a
-    const bool in_b = (executed & 1) != 0;
-    grid_copy_bytes(in_b ? f.keys_a : f.keys_b, in_b ? f.keys_b : f.keys_a, f.key_bytes_total);
-    if (f.val_bytes_total) grid_copy_bytes(in_b ? f.vals_a : f.vals_b, in_b ? f.vals_b : f.vals_a, f.val_bytes_total);
+    fixup_body(f);
 }
 thread_local std::string g_last_error;
 
@@ -284,6 +272,8 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     // short arrays take the small-tile shape (always 32-bit status words)
     const bool small = n <= SMALL_N_MAX && !p.wide_status;
     p.pass = pass_entries(p.kb)[vi * 3 + (small ? 2 : p.wide_status ? 1 : 0)];
+    // short keys-only arrays: one cooperative launch of the same pass shape
+    if (small && p.vb == 0 && g_short_fused.load(std::memory_order_relaxed)) p.fused = *fused_entry(p.kb);
     p.upsweep = *upsweep_entry(p.kb);
     const uint64_t tiles = (n + uint64_t(p.pass.tile) - 1) / uint64_t(p.pass.tile);
     if (tiles > 0xFFFFFFFFull) return GBSORT_ERR_INVALID_ARGUMENT;
@@ -358,35 +348,8 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         return GBSORT_ERR_CUDA;
     };
 
-    cudaError_t e = cudaMemsetAsync(ctl, 0, plan.ctl.bytes, stream);
-    if (e != cudaSuccess) return fail("memset control block", e);
-
-    HistParams hp{};
-    hp.keys = copy ? keys_src : d_keys;
-    hp.n = plan.n;
-    hp.kind = plan.kind;
-    hp.desc = descending;
-    hp.gp_counts = gp;
-    hp.status = status;
-    hp.status_bytes = plan.status_bytes;
-    hp.mirror_keys = odd ? alt_keys : nullptr;
-    hp.vals = copy ? vals_src : d_values;
-    hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
-    hp.val_bytes_total = plan.n * uint64_t(plan.vb);
-    const uint32_t hist_ctas = upsweep_ctas(plan.n, plan.kb);
-    {
-        void* args[] = {&hp};
-        if (timed) cudaEventRecord(ev[0], stream);
-        e = cudaLaunchKernel(plan.upsweep.fn, dim3(hist_ctas), dim3(plan.upsweep.threads), args,
-                             plan.upsweep.smem, stream);
-        if (e != cudaSuccess) return fail("upsweep launch", e);
-        if (timed) cudaEventRecord(ev[1], stream);
-    }
-
-    const int occ = resident_ctas(plan.pass);
-    const uint64_t max_ctas = uint64_t(sms) * uint64_t(occ > 0 ? occ : 1);
-    const uint32_t pass_ctas = uint32_t(plan.num_tiles < max_ctas ? plan.num_tiles : max_ctas);
-    for (int pass = 0; pass < plan.passes; ++pass) {
+    // Parameters of digit pass `pass` and of the fix-up copy.
+    auto pass_params = [&](int pass) {
         // Even passes read the user's buffer unless the mirror made the
         // alternate buffer the source (odd pass counts end in place).
         const bool from_user = ((pass + (odd ? 1 : 0)) & 1) == 0;
@@ -421,12 +384,9 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         pp.copy_keys_in = copy ? keys_src : nullptr;
         pp.copy_vals_in = copy ? vals_src : nullptr;
         pp.executed = fixup ? reinterpret_cast<uint32_t*>(ctl + plan.ctl.exec_off) : nullptr;
-        void* args[] = {&pp};
-        e = launch_dependent(plan.pass.fn, pass_ctas, plan.pass.threads, plan.pass.smem, stream, args);
-        if (e != cudaSuccess) return fail("pass launch", e);
-        if (timed) cudaEventRecord(ev[2 + pass], stream);
-    }
-    if (fixup) {
+        return pp;
+    };
+    auto fixup_params = [&] {
         FixupParams fp{};
         fp.executed = reinterpret_cast<const uint32_t*>(ctl + plan.ctl.exec_off);
         fp.passes = plan.passes;
@@ -439,6 +399,77 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         fp.copy_keys_in = copy ? keys_src : nullptr;
         fp.copy_vals_in = copy ? vals_src : nullptr;
         fp.want_odd = alt ? (plan.passes & 1) : 0;
+        return fp;
+    };
+
+    cudaError_t e = cudaMemsetAsync(ctl, 0, plan.ctl.bytes, stream);
+    if (e != cudaSuccess) return fail("memset control block", e);
+
+    HistParams hp{};
+    hp.keys = copy ? keys_src : d_keys;
+    hp.n = plan.n;
+    hp.kind = plan.kind;
+    hp.desc = descending;
+    hp.gp_counts = gp;
+    hp.status = status;
+    hp.status_bytes = plan.status_bytes;
+    hp.mirror_keys = odd ? alt_keys : nullptr;
+    hp.vals = copy ? vals_src : d_values;
+    hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
+    hp.val_bytes_total = plan.n * uint64_t(plan.vb);
+    if (plan.fused.fn != nullptr && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0) {
+        // Short array: the whole sort in one cooperative launch (every CTA
+        // resident, or the launch fails; fused_short.cuh).
+        FusedParams f{};
+        f.hist = hp;
+        f.pass = pass_params(0);
+        if (fixup) f.fix = fixup_params();
+        f.fixup = fixup ? 1 : 0;
+        f.barrier = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_off);
+        const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
+        const uint32_t grid = uint32_t(plan.num_tiles < fmax ? plan.num_tiles : fmax);
+        void* args[] = {&f};
+        if (timed) cudaEventRecord(ev[0], stream);
+        e = cudaLaunchCooperativeKernel(plan.fused.fn, dim3(grid), dim3(plan.fused.threads), args, plan.fused.smem,
+                                        stream);
+        if (e == cudaSuccess) {
+            if (timed) {
+                cudaEventRecord(ev[1], stream);
+                e = cudaEventSynchronize(ev[1]);
+                if (e != cudaSuccess) return fail("event sync", e);
+                float t = 0.f;
+                cudaEventElapsedTime(&t, ev[0], ev[1]);
+                if (ms_cap > 0) ms[0] = t;
+                if (n_ms) *n_ms = ms_cap > 0 ? 1 : 0;
+                for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
+            }
+            return GBSORT_OK;
+        }
+        if (e != cudaErrorCooperativeLaunchTooLarge) return fail("one-launch sort", e);
+        cudaGetLastError();  // the grid cannot be resident at once here: the multi-launch path follows
+    }
+    const uint32_t hist_ctas = upsweep_ctas(plan.n, plan.kb);
+    {
+        void* args[] = {&hp};
+        if (timed) cudaEventRecord(ev[0], stream);
+        e = cudaLaunchKernel(plan.upsweep.fn, dim3(hist_ctas), dim3(plan.upsweep.threads), args,
+                             plan.upsweep.smem, stream);
+        if (e != cudaSuccess) return fail("upsweep launch", e);
+        if (timed) cudaEventRecord(ev[1], stream);
+    }
+
+    const int occ = resident_ctas(plan.pass);
+    const uint64_t max_ctas = uint64_t(sms) * uint64_t(occ > 0 ? occ : 1);
+    const uint32_t pass_ctas = uint32_t(plan.num_tiles < max_ctas ? plan.num_tiles : max_ctas);
+    for (int pass = 0; pass < plan.passes; ++pass) {
+        PassParams pp = pass_params(pass);
+        void* args[] = {&pp};
+        e = launch_dependent(plan.pass.fn, pass_ctas, plan.pass.threads, plan.pass.smem, stream, args);
+        if (e != cudaSuccess) return fail("pass launch", e);
+        if (timed) cudaEventRecord(ev[2 + pass], stream);
+    }
+    if (fixup) {
+        FixupParams fp = fixup_params();
         void* args[] = {&fp};
         e = launch_dependent(reinterpret_cast<const void*>(&skip_fixup_kernel), uint32_t(sms > 0 ? sms : 1), 256, 0,
                              stream, args);
@@ -498,14 +529,14 @@ int check_args(int key_type, size_t value_bytes, void* d_keys, void* d_values, s
 // graph, if any, is destroyed; one still running is freed by CUDA when it
 // completes).  gbsort_graph_cache_clear() frees them all.
 struct GraphKey {
-    int device, key_type, desc, skip;
+    int device, key_type, desc, skip, fused;
     size_t vb;
     uint64_t n, wait_limit;
     const void *keys, *vals, *ws, *ksrc, *vsrc, *keys_b, *vals_b;
     cudaStream_t stream;
     auto tie() const {
-        return std::tie(device, key_type, desc, skip, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc, keys_b, vals_b,
-                        stream);
+        return std::tie(device, key_type, desc, skip, fused, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc, keys_b,
+                        vals_b, stream);
     }
     bool operator==(const GraphKey& o) const { return tie() == o.tie(); }
 };
@@ -542,6 +573,7 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
     k.key_type = plan.key_type;
     k.desc = descending;
     k.skip = g_pass_skip.load(std::memory_order_relaxed);
+    k.fused = plan.fused.fn != nullptr;
     k.vb = size_t(plan.vb);
     k.n = plan.n;
     k.wait_limit = wait_limit_ns();
@@ -880,6 +912,8 @@ void gbsort_graph_cache_stats(uint64_t* calls, uint64_t* graphs, uint64_t* captu
 
 void gbsort_set_pass_skip(int enable) { g_pass_skip.store(enable ? 1 : 0, std::memory_order_relaxed); }
 int gbsort_get_pass_skip(void) { return g_pass_skip.load(std::memory_order_relaxed); }
+void gbsort_set_short_fused(int enable) { g_short_fused.store(enable ? 1 : 0, std::memory_order_relaxed); }
+int gbsort_get_short_fused(void) { return g_short_fused.load(std::memory_order_relaxed); }
 
 void gbsort_set_wait_limit_ns(uint64_t ns) { g_wait_limit_ns.store(ns, std::memory_order_relaxed); }
 uint64_t gbsort_get_wait_limit_ns(void) { return wait_limit_ns(); }
@@ -904,6 +938,12 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
     }
     out->status_word_bytes = plan.wide_status ? 8 : 4;
     out->kernel_launches = uint32_t(plan.passes + 1 + ((gbsort_get_pass_skip() && (plan.passes & 1) == 0) ? 1 : 0));
+    if (plan.fused.fn && sms > 0 && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0) {
+        const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
+        out->pass_ctas = uint32_t(plan.num_tiles < fmax ? plan.num_tiles : fmax);
+        out->hist_ctas = 0;  // counted by the same launch
+        out->kernel_launches = 1;
+    }
     out->workspace_bytes = plan.total_bytes;
     return GBSORT_OK;
 }

@@ -95,6 +95,17 @@ struct FixupParams {
     const void* copy_vals_in;
 };
 
+// One-launch sort of a short array (cooperative launch, every CTA resident):
+// digit counts of all passes, then every pass, then the parity fix-up, with a
+// grid barrier between the phases.
+struct FusedParams {
+    HistParams hist;        // phase 0 (status clear, mirror for odd pass counts)
+    PassParams pass;        // pass 0; the kernel derives each later pass from it
+    FixupParams fix;
+    int fixup;              // run the fix-up phase
+    uint32_t* barrier;      // grid barrier counter, zeroed before the launch
+};
+
 // Batched upsweep: one work item per chunk of one segment.
 struct SegItem {
     unsigned long long begin, end;  // element range (within one segment)

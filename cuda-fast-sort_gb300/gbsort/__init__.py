@@ -92,6 +92,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "gbsort_set_wait_limit_ns": (None, [u64]),
         "gbsort_get_wait_limit_ns": (u64, []),
         "gbsort_probe_wait_timeout": (i, [vp, u64, vp]),
+        "gbsort_probe_barrier_timeout": (i, [vp, u64, vp]),
         "gbsort_plan": (i, [i, sz, sz, ctypes.POINTER(PlanInfo)]),
         "gbsort_sort_timed": (i, [i, i, vp, vp, sz, vp, sz, sz, vp, ctypes.POINTER(ctypes.c_float), i,
                                   ctypes.POINTER(ctypes.c_int)]),
@@ -268,6 +269,10 @@ def get_wait_limit_ns() -> int:
 
 def probe_wait_timeout(scratch, limit_ns: int, stream=None) -> int:
     return lib().gbsort_probe_wait_timeout(_ptr(scratch), limit_ns, _stream(stream))
+
+
+def probe_barrier_timeout(scratch, limit_ns: int, stream=None) -> int:
+    return lib().gbsort_probe_barrier_timeout(_ptr(scratch), limit_ns, _stream(stream))
 
 
 def sm_count() -> int:
@@ -573,6 +578,20 @@ def set_pass_skip(enable: bool) -> None:
 
 def get_pass_skip() -> bool:
     f = lib().gbsort_get_pass_skip
+    f.restype = ctypes.c_int
+    return bool(f())
+
+
+def set_short_fused(enable: bool) -> None:
+    """One-launch sort of short keys-only arrays on (default) or off."""
+    f = lib().gbsort_set_short_fused
+    f.restype = None
+    f.argtypes = [ctypes.c_int]
+    f(int(enable))
+
+
+def get_short_fused() -> bool:
+    f = lib().gbsort_get_short_fused
     f.restype = ctypes.c_int
     return bool(f())
 

@@ -454,6 +454,17 @@ int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n,
 void gbsort_set_pass_skip(int enable);
 int gbsort_get_pass_skip(void);
 
+/* One-launch sort of short keys-only arrays (n <= 2^22, no values; plain,
+ * input-preserving and DoubleBuffer forms): the digit counts, every pass and
+ * the pass-skip fix-up run in one cooperative launch with a grid barrier
+ * (bounded wait, GBSORT_ERR_TIMEOUT) between them, instead of one launch per
+ * kernel.  The reference's short mode (radix_kernel.cuh:525-559) still
+ * launches every kernel.  Off by default (GBSORT_SHORT_FUSED=1 in the
+ * environment or gbsort_set_short_fused(1) selects it).  Results are
+ * identical either way. */
+void gbsort_set_short_fused(int enable);
+int gbsort_get_short_fused(void);
+
 /* Graph replay of repeated calls (default on; GBSORT_GRAPH_CACHE=0 turns it
  * off at load).  The second call of gbsort_sort_keys / _pairs / _copy with
  * the same buffers, size, key type, order, stream and settings is captured
@@ -484,6 +495,14 @@ uint64_t gbsort_get_wait_limit_ns(void);
  * lookback without stalling any sort. */
 int gbsort_probe_wait_timeout(void* d_scratch, uint64_t limit_ns,
                               void* stream);
+
+/* Runs the grid barrier of the one-launch short sort, on the device, where
+ * the second arrival it waits for never comes, with the given limit; returns
+ * GBSORT_ERR_TIMEOUT when the wait gave up (the expected outcome) and
+ * GBSORT_OK otherwise.  d_scratch must point to 64 bytes of device memory.
+ * Exercises that barrier's failure path without stalling any sort. */
+int gbsort_probe_barrier_timeout(void* d_scratch, uint64_t limit_ns,
+                                 void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Result checks on the device (the reference's post-sort checks,           */
@@ -519,7 +538,8 @@ typedef struct gbsort_plan_info {
     uint32_t pass_ctas;       /* persistent CTAs of the pass kernel          */
     uint32_t hist_ctas;       /* CTAs of the histogram kernel                */
     uint32_t status_word_bytes; /* 4 or 8                                    */
-    uint32_t kernel_launches; /* launches (plus one memset node) per sort    */
+    uint32_t kernel_launches; /* launches (plus one memset node) per sort;
+                                 1 when a short array sorts in one launch     */
     uint64_t workspace_bytes;
 } gbsort_plan_info;
 
@@ -530,7 +550,9 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n,
  * records a CUDA event around every kernel on `stream` and, after
  * synchronizing, writes the per-kernel device milliseconds to ms_out:
  * ms_out[0] = histogram kernel, ms_out[1 + p] = digit pass p, and with pass
- * skipping on and an even pass count P, ms_out[1 + P] = the fix-up copy.  ms_cap is the
+ * skipping on and an even pass count P, ms_out[1 + P] = the fix-up copy.  A
+ * short array sorted in one launch (gbsort_set_short_fused) writes one entry,
+ * the whole sort.  ms_cap is the
  * capacity of ms_out; *n_ms receives the number of entries written. */
 int gbsort_sort_timed(int key_type, int descending, void* d_keys,
                       void* d_values, size_t value_bytes, void* d_workspace,

@@ -1,0 +1,115 @@
+"""One-launch sort of short keys-only arrays (fused_short.cuh): the digit
+counts, every pass and the fix-up in one cooperative launch with a bounded
+grid barrier between them.
+
+Every other GPU test of keys-only arrays up to 2^22 keys already runs through
+this path (it is the default).  Here:
+  - the plan reports one launch up to 2^22 keys and the multi-launch path
+    above, and both sides of the switch equal the oracle;
+  - the one-launch and multi-launch paths give identical bytes for every key
+    type, both orders, and for inputs whose uniform digits skip passes;
+  - the grid barrier's bounded wait runs out on a barrier nothing completes
+    (GBSORT_ERR_TIMEOUT) and the context stays usable;
+  - a one-launch sort whose waits all run out (1 ns limit) reports
+    GBSORT_ERR_TIMEOUT, and the next sort is correct.
+"""
+
+import numpy as np
+import pytest
+
+from _oracle import KEY_TYPES, raw_keys
+from gpu_util import gpu_sort, from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+SMALL_MAX = 1 << 22
+
+
+def _eq(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
+
+
+@pytest.fixture
+def fused_default(gb):
+    old = gb.get_short_fused()
+    gb.set_short_fused(True)
+    yield
+    gb.set_short_fused(old)
+
+
+@pytest.mark.parametrize("n", [1, 100, 4095, 4096, 4097, 1 << 20, SMALL_MAX - 1, SMALL_MAX, SMALL_MAX + 1])
+def test_plan_switch_and_oracle(gb, cuda, oracle, fused_default, n):
+    info = gb.plan("u32", n)
+    if n <= SMALL_MAX:
+        assert info.kernel_launches == 1 and info.hist_ctas == 0
+    else:
+        assert info.kernel_launches > 1
+    raw = raw_keys("u32", n, seed=n % 1000 + 3)
+    assert _eq(gpu_sort(gb, cuda, "u32", raw), oracle.sort("u32", raw, False))
+
+
+def test_values_and_long_arrays_keep_the_multi_launch_path(gb, fused_default):
+    assert gb.plan("u32", 1 << 20, 4).kernel_launches > 1
+    assert gb.plan("u64", SMALL_MAX + 1).kernel_launches > 1
+
+
+def _both_paths(gb, cuda, kt, raw, desc):
+    gb.set_short_fused(True)
+    one = gpu_sort(gb, cuda, kt, raw, desc)
+    gb.set_short_fused(False)
+    try:
+        multi = gpu_sort(gb, cuda, kt, raw, desc)
+    finally:
+        gb.set_short_fused(True)
+    return one, multi
+
+
+@pytest.mark.parametrize("kt", KEY_TYPES)
+@pytest.mark.parametrize("desc", [False, True])
+def test_one_launch_equals_multi_launch(gb, cuda, oracle, fused_default, kt, desc):
+    raw = raw_keys(kt, 300_007, seed=11 + len(kt))
+    one, multi = _both_paths(gb, cuda, kt, raw, desc)
+    assert _eq(one, multi)
+    assert _eq(one, oracle.sort(kt, raw, desc))
+
+
+@pytest.mark.parametrize("kt,dist", [("u32", 5), ("u64", 5), ("u16", 3), ("u128", 3)])
+def test_one_launch_with_skipped_passes(gb, cuda, oracle, fused_default, kt, dist):
+    raw = raw_keys(kt, 123_457, seed=5, dist=dist)  # constant bytes: their passes are skipped
+    one, multi = _both_paths(gb, cuda, kt, raw, False)
+    assert _eq(one, multi)
+    assert _eq(one, oracle.sort(kt, raw, False))
+
+
+def test_grid_barrier_wait_runs_out(gb, cuda):
+    scratch = cuda.empty(64, dtype=cuda.uint8, device="cuda")
+    assert gb.probe_barrier_timeout(scratch, 2_000_000) == gb.ERR_TIMEOUT  # 2 ms
+    cuda.cuda.synchronize()
+    x = cuda.arange(10, device="cuda")
+    assert int(x.sum().item()) == 45  # the context is still usable
+
+
+def test_one_launch_reports_timed_out_waits(gb, cuda, oracle, fused_default):
+    n = 1 << 20
+    assert gb.plan("u32", n).kernel_launches == 1
+    raw = raw_keys("u32", n, seed=77)
+    tb = gb.temp_bytes("u32", n)
+    ws = cuda.empty(tb, dtype=cuda.uint8, device="cuda")
+    old = gb.get_wait_limit_ns()
+    seen = gb.OK
+    try:
+        gb.set_wait_limit_ns(1)
+        for _ in range(3):
+            d = to_dev(cuda, raw)
+            gb.sort(d, n, "u32", ws, tb)
+            seen = gb.workspace_status("u32", n, ws)
+            if seen != gb.OK:
+                break
+    finally:
+        gb.set_wait_limit_ns(old)
+    assert seen == gb.ERR_TIMEOUT, gb.status_string(seen)
+    d = to_dev(cuda, raw)
+    gb.sort(d, n, "u32", ws, tb)
+    cuda.cuda.synchronize()
+    assert gb.workspace_status("u32", n, ws) == gb.OK
+    assert _eq(from_dev(d, raw), oracle.sort("u32", raw, False))
