@@ -318,10 +318,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
-    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -392,29 +388,33 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 
 // Grid-wide barrier of a cooperative launch (every CTA resident at once).
-// `counter` starts at 0; the k-th barrier of the launch (k = 1, 2, ...) waits
-// until it reaches k * gridDim.x.  Thread 0 of each CTA arrives with a
-// release and waits with acquire loads, bounded by limit_ns: a wait that runs
-// out records ERRBIT_TIMEOUT and the barrier returns false on every thread
-// of that CTA, so the caller can leave instead of hanging.
-__device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t k, uint64_t limit_ns, uint32_t* err) {
+// counter and gen start at 0 (gen in another 128-byte line, so the waiting
+// CTAs' polls do not queue behind the arrivals' atomics).  The k-th barrier
+// of the launch (k = 1, 2, ...): thread 0 of each CTA arrives with a release
+// (atomicAdd on counter); the CTA that brings counter to k * gridDim.x
+// publishes gen = k; the others poll gen with acquire loads, bounded by
+// limit_ns: a wait that runs out records ERRBIT_TIMEOUT and the barrier
+// returns false on every thread of that CTA, so the caller can leave
+// instead of hanging.
+__device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t* gen, uint32_t k, uint64_t limit_ns,
+                                             uint32_t* err) {
     __syncthreads();
     int ok = 1;
     if (threadIdx.x == 0) {
-        const uint32_t target = k * gridDim.x;
         __threadfence();
-        atomicAdd(counter, 1u);
-        if (ld_acquire(counter) < target) {
+        const uint32_t arrived = atomicAdd(counter, 1u) + 1u;
+        if (arrived == k * gridDim.x) {
+            __threadfence();
+            asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(k) : "memory");
+        } else if (ld_acquire(gen) < k) {
             const uint64_t t0 = global_timer_ns();
-            uint32_t sleep_ns = 32;
-            while (ld_acquire(counter) < target) {
+            while (ld_acquire(gen) < k) {
                 if (global_timer_ns() - t0 > limit_ns) {
                     atomicOr(err, ERRBIT_TIMEOUT);
                     ok = 0;
                     break;
                 }
-                __nanosleep(sleep_ns);
-                if (sleep_ns < 256) sleep_ns <<= 1;
+                __nanosleep(32);
             }
         }
         __threadfence();

@@ -124,7 +124,8 @@ __global__ void probe_wait_kernel(uint32_t* scratch, uint64_t limit_ns) {
 __global__ void probe_barrier_kernel(uint32_t* scratch, uint64_t limit_ns) {
     uint32_t* counter = scratch;
     uint32_t* err = scratch + 1;
-    (void)grid_barrier(counter, 2u, limit_ns, err);
+    uint32_t* gen = scratch + 8;
+    (void)grid_barrier(counter, gen, 2u, limit_ns, err);
 }
 
 }  // namespace

@@ -46,12 +46,12 @@ const KernelEntry* pass_entries_for() {
 // The one-launch sort of short keys-only arrays, in the short-array pass shape.
 template <int KB>
 const KernelEntry* fused_entry_for() {
-    using S = PassShapeSmall<KB, 0>;
-    using G = PassGeom<KB, 0, S::THREADS, S::IPT>;
+    using S = FusedShape<KB>;
+    using G = ShortGeom<KB, S::THREADS, S::IPT>;
+    static_assert(G::TILE == PassShapeSmall<KB, 0>::THREADS * PassShapeSmall<KB, 0>::IPT, "same tiles as the short shape");
     static const KernelEntry e = {
-        reinterpret_cast<const void*>(
-            &fused_short_kernel<KB, uint32_t, S::THREADS, S::IPT, S::MIN_CTAS, S::LOOKBACK_WINDOW>),
-        S::THREADS, S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
+        reinterpret_cast<const void*>(&fused_short_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
+        G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
     return &e;
 }
 

@@ -196,12 +196,8 @@ struct PassGeom {
 // count), each segment's first tile publishes an inclusive prefix of its own
 // so lookback chains never cross segments, and digit bases come per segment
 // from p.seg_gofs.
-// The pass as a device function: the pass kernel below runs it once; the
-// one-launch short sort (fused_short.cuh) runs it once per digit pass with a
-// grid barrier in between.  REUSE: the CTA runs further passes after this
-// one, so the mbarriers are invalidated on the way out (a clean exit, or one
-// that drained its copies after an error) and initialised again next time.
-template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int LBW, bool REUSE = false>
+// The pass as a device function, run once by the pass kernel below.
+template <int KB, int VB, class W, int THREADS, int IPT, bool SEG, int LBW>
 __device__ __forceinline__ void onesweep_pass_body(const PassParams& p, uint8_t* smem) {
     using U = typename KeyBits<KB>::U;
     using V = typename ValBits<VB>::V;
@@ -500,11 +496,6 @@ __device__ __forceinline__ void onesweep_pass_body(const PassParams& p, uint8_t*
                 mbar_wait_bounded(&mbar[b], ((parity >> b) & 1u) ^ 1u, DRAIN_LIMIT_NS, p.err);
                 if (next_issued) mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
                 if constexpr (G::LATE) mbar_wait_bounded(&mbar[2], vparity, DRAIN_LIMIT_NS, p.err);
-                if constexpr (REUSE) {
-                    mbar_inval(&mbar[0]);
-                    mbar_inval(&mbar[1]);
-                    mbar_inval(&mbar[2]);
-                }
             }
             return;
         }
@@ -691,11 +682,6 @@ __device__ __forceinline__ void onesweep_pass_body(const PassParams& p, uint8_t*
                     mbar_wait_bounded(&mbar[2], vparity ^ 1u, DRAIN_LIMIT_NS, p.err);
                     if (next_issued)
                         mbar_wait_bounded(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, DRAIN_LIMIT_NS, p.err);
-                    if constexpr (REUSE) {
-                        mbar_inval(&mbar[0]);
-                        mbar_inval(&mbar[1]);
-                        mbar_inval(&mbar[2]);
-                    }
                 }
                 return;
             }
@@ -704,14 +690,6 @@ __device__ __forceinline__ void onesweep_pass_body(const PassParams& p, uint8_t*
         }
         cur = next_info;
         ++it;
-    }
-    if constexpr (REUSE) {
-        __syncthreads();  // no thread still waits on a barrier
-        if (tid == 0) {
-            mbar_inval(&mbar[0]);
-            mbar_inval(&mbar[1]);
-            mbar_inval(&mbar[2]);
-        }
     }
 }
 

@@ -15,6 +15,7 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Control block at the start of the workspace's control region:
 //   [gp_counts: passes*256 u64][tile_counters: 16 u32][err: u32][executed: u32][barrier: u32][pad]
+//   [barrier generation: u32, own 128-byte line][pad]
 // executed: written by the pass kernels that run (bit 31 | passes executed)
 // when uniform passes are skipped; 0 when none ran.
 struct CtlLayout {
@@ -22,7 +23,8 @@ struct CtlLayout {
     size_t counters_off = 0;
     size_t err_off = 0;
     size_t exec_off = 0;
-    size_t barrier_off = 0;  // grid barrier counter of the one-launch short sort
+    size_t barrier_off = 0;      // grid barrier counter of the one-launch short sort
+    size_t barrier_gen_off = 0;  // its generation word (another 128-byte line)
     size_t bytes = 0;
     static CtlLayout make(int passes) {
         CtlLayout c;
@@ -31,7 +33,8 @@ struct CtlLayout {
         c.err_off = c.counters_off + 16 * 4;
         c.exec_off = c.err_off + 4;
         c.barrier_off = c.exec_off + 4;
-        c.bytes = align_up(c.barrier_off + 4, 256);
+        c.barrier_gen_off = align_up(c.barrier_off + 4, 128);
+        c.bytes = align_up(c.barrier_gen_off + 4, 256);
         return c;
     }
 };

@@ -53,6 +53,23 @@ constexpr ShapeRow pass_shape_small_row(int kb, int vb) {
 }
 constexpr uint64_t SMALL_N_MAX = uint64_t(1) << 22;
 
+// Arrays sorted in one launch when keys-only (fused_short.cuh): up to 2^21
+// keys.  Measured on GB300 (u32, CUDA events): 2^16 40.8 vs 59.0 us, 2^20
+// 56-58 vs 76.6 us (graph replay of the separate launches: 62 us), 2^22
+// 164.8 vs 157.4 us, so longer arrays keep the separate launches.
+constexpr uint64_t FUSED_N_MAX = uint64_t(1) << 21;
+
+// The one-launch short sort: the short shape's tile, ranked by 512 threads
+// where it divides (half the columns per warp: a shorter dependent chain in
+// the rank, which bounds a short sort's passes).
+template <int KB>
+struct FusedShape {
+    static constexpr int TILE = pass_shape_small_row(KB, 0).threads * pass_shape_small_row(KB, 0).ipt;
+    static constexpr int THREADS = TILE % 512 == 0 ? 512 : pass_shape_small_row(KB, 0).threads;
+    static constexpr int IPT = TILE / THREADS;
+    static constexpr int MIN_CTAS = pass_shape_small_row(KB, 0).min_ctas;
+};
+
 // Predecessor tiles per lookback round trip for short arrays: all their tiles
 // are in flight at once, so the known-prefix frontier moves a window per L2
 // round trip (2^20 u32: 4 -> 8 took 14.0 -> 14.35 Gkeys/s; 16 and 32 slower).

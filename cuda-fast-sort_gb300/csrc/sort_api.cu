@@ -24,6 +24,7 @@
 #include "gbsort.h"
 #include "plan.h"
 #include "device_common.cuh"
+#include "fused_short.cuh"
 #include "onesweep.cuh"
 #include "sort_params.h"
 
@@ -81,11 +82,11 @@ const KernelEntry* upsweep_entry(int kb) {
 namespace {
 
 std::atomic<uint64_t> g_wait_limit_ns{2000000000ull};
-// One-launch sort of short keys-only arrays: off unless GBSORT_SHORT_FUSED=1
-// or switched on (gbsort_set_short_fused).
+// One-launch sort of short keys-only arrays: on unless GBSORT_SHORT_FUSED=0
+// or switched off (gbsort_set_short_fused).
 std::atomic<int> g_short_fused{[] {
     const char* v = std::getenv("GBSORT_SHORT_FUSED");
-    return (v && v[0] == '1') ? 1 : 0;
+    return (v && v[0] == '0') ? 0 : 1;
 }()};
 // Uniform-digit pass skipping: on unless GBSORT_PASS_SKIP=0 or switched off.
 std::atomic<int> g_pass_skip{[] {
@@ -273,7 +274,8 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     const bool small = n <= SMALL_N_MAX && !p.wide_status;
     p.pass = pass_entries(p.kb)[vi * 3 + (small ? 2 : p.wide_status ? 1 : 0)];
     // short keys-only arrays: one cooperative launch of the same pass shape
-    if (small && p.vb == 0 && g_short_fused.load(std::memory_order_relaxed)) p.fused = *fused_entry(p.kb);
+    if (small && n <= FUSED_N_MAX && p.vb == 0 && g_short_fused.load(std::memory_order_relaxed))
+        p.fused = *fused_entry(p.kb);
     p.upsweep = *upsweep_entry(p.kb);
     const uint64_t tiles = (n + uint64_t(p.pass.tile) - 1) / uint64_t(p.pass.tile);
     if (tiles > 0xFFFFFFFFull) return GBSORT_ERR_INVALID_ARGUMENT;
@@ -287,7 +289,9 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     p.ctl_off = off;
     off = align_up(off + p.ctl.bytes, 256);
     p.status_off = off;
-    p.status_bytes = size_t(p.num_tiles) * 256 * (p.wide_status ? 8 : 4);
+    // short arrays: room for the one-launch sort's group sums too, so the
+    // size query does not depend on which short path runs
+    p.status_bytes = small ? short_status_words(p.num_tiles) * 4 : size_t(p.num_tiles) * 256 * (p.wide_status ? 8 : 4);
     off = align_up(off + p.status_bytes, 256);
     p.total_bytes = off;
     *plan = p;
@@ -426,6 +430,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         if (fixup) f.fix = fixup_params();
         f.fixup = fixup ? 1 : 0;
         f.barrier = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_off);
+        f.barrier_gen = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_gen_off);
         const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
         const uint32_t grid = uint32_t(plan.num_tiles < fmax ? plan.num_tiles : fmax);
         void* args[] = {&f};

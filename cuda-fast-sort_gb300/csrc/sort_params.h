@@ -103,7 +103,8 @@ struct FusedParams {
     PassParams pass;        // pass 0; the kernel derives each later pass from it
     FixupParams fix;
     int fixup;              // run the fix-up phase
-    uint32_t* barrier;      // grid barrier counter, zeroed before the launch
+    uint32_t* barrier;      // grid barrier counter and generation, zeroed before the launch
+    uint32_t* barrier_gen;
 };
 
 // Batched upsweep: one work item per chunk of one segment.

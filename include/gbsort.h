@@ -454,14 +454,14 @@ int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n,
 void gbsort_set_pass_skip(int enable);
 int gbsort_get_pass_skip(void);
 
-/* One-launch sort of short keys-only arrays (n <= 2^22, no values; plain,
+/* One-launch sort of short keys-only arrays (n <= 2^21, no values; plain,
  * input-preserving and DoubleBuffer forms): the digit counts, every pass and
  * the pass-skip fix-up run in one cooperative launch with a grid barrier
  * (bounded wait, GBSORT_ERR_TIMEOUT) between them, instead of one launch per
  * kernel.  The reference's short mode (radix_kernel.cuh:525-559) still
- * launches every kernel.  Off by default (GBSORT_SHORT_FUSED=1 in the
- * environment or gbsort_set_short_fused(1) selects it).  Results are
- * identical either way. */
+ * launches every kernel.  On by default; GBSORT_SHORT_FUSED=0 in the
+ * environment or gbsort_set_short_fused(0) selects the separate launches.
+ * Results are identical either way. */
 void gbsort_set_short_fused(int enable);
 int gbsort_get_short_fused(void);
 

@@ -2,9 +2,9 @@
 counts, every pass and the fix-up in one cooperative launch with a bounded
 grid barrier between them.
 
-Every other GPU test of keys-only arrays up to 2^22 keys already runs through
+Every other GPU test of keys-only arrays up to 2^21 keys already runs through
 this path (it is the default).  Here:
-  - the plan reports one launch up to 2^22 keys and the multi-launch path
+  - the plan reports one launch up to 2^21 keys and the multi-launch path
     above, and both sides of the switch equal the oracle;
   - the one-launch and multi-launch paths give identical bytes for every key
     type, both orders, and for inputs whose uniform digits skip passes;
@@ -22,7 +22,7 @@ from gpu_util import gpu_sort, from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
 
-SMALL_MAX = 1 << 22
+FUSED_MAX = 1 << 21
 
 
 def _eq(a, b):
@@ -37,10 +37,10 @@ def fused_default(gb):
     gb.set_short_fused(old)
 
 
-@pytest.mark.parametrize("n", [1, 100, 4095, 4096, 4097, 1 << 20, SMALL_MAX - 1, SMALL_MAX, SMALL_MAX + 1])
+@pytest.mark.parametrize("n", [1, 100, 4095, 4096, 4097, 1 << 20, FUSED_MAX - 1, FUSED_MAX, FUSED_MAX + 1])
 def test_plan_switch_and_oracle(gb, cuda, oracle, fused_default, n):
     info = gb.plan("u32", n)
-    if n <= SMALL_MAX:
+    if n <= FUSED_MAX:
         assert info.kernel_launches == 1 and info.hist_ctas == 0
     else:
         assert info.kernel_launches > 1
@@ -50,7 +50,7 @@ def test_plan_switch_and_oracle(gb, cuda, oracle, fused_default, n):
 
 def test_values_and_long_arrays_keep_the_multi_launch_path(gb, fused_default):
     assert gb.plan("u32", 1 << 20, 4).kernel_launches > 1
-    assert gb.plan("u64", SMALL_MAX + 1).kernel_launches > 1
+    assert gb.plan("u64", FUSED_MAX + 1).kernel_launches > 1
 
 
 def _both_paths(gb, cuda, kt, raw, desc):
