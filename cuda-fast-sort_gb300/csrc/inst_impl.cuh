@@ -47,11 +47,11 @@ const KernelEntry* pass_entries_for() {
 template <int KB>
 const KernelEntry* fused_entry_for() {
     using S = FusedShape<KB>;
-    using G = ShortGeom<KB, S::THREADS, S::IPT>;
+    using G = ShortGeom<KB, S::THREADS, S::IPT, S::LIPT>;
     static_assert(G::TILE == PassShapeSmall<KB, 0>::THREADS * PassShapeSmall<KB, 0>::IPT, "same tiles as the short shape");
     static const KernelEntry e = {
-        reinterpret_cast<const void*>(&fused_short_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
-        G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
+        reinterpret_cast<const void*>(&fused_short_kernel<KB, S::THREADS, S::IPT, S::LIPT, S::MIN_CTAS>), S::THREADS,
+        S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
     return &e;
 }
 

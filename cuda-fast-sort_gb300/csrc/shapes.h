@@ -54,10 +54,14 @@ constexpr ShapeRow pass_shape_small_row(int kb, int vb) {
 constexpr uint64_t SMALL_N_MAX = uint64_t(1) << 22;
 
 // Arrays sorted in one launch when keys-only (fused_short.cuh): up to 2^21
-// keys.  Measured on GB300 (u32, CUDA events): 2^16 40.8 vs 59.0 us, 2^20
-// 56-58 vs 76.6 us (graph replay of the separate launches: 62 us), 2^22
-// 164.8 vs 157.4 us, so longer arrays keep the separate launches.
+// keys (2^20 for 16-byte keys, whose buckets outgrow a CTA sooner and whose
+// 16 passes then run slower inside one launch: 2^21 u128 610 vs 567 us).
+// With every digit taking a pass inside the launch, u32 measured (CUDA
+// events) 2^16 40.8 vs 59.0 us, 2^20 56-58 vs 76.6, 2^22 164.8 vs 157.4;
+// with the MSD partition + bucket sorts, 2^17 28.6 vs 62.5, 2^20 36.6 vs
+// 76.6, 2^21 98 vs 111.
 constexpr uint64_t FUSED_N_MAX = uint64_t(1) << 21;
+constexpr uint64_t fused_n_max(int kb) { return kb == 16 ? FUSED_N_MAX / 2 : FUSED_N_MAX; }
 
 // The one-launch short sort: the short shape's tile, ranked by 512 threads
 // where it divides (half the columns per warp: a shorter dependent chain in
@@ -68,6 +72,10 @@ struct FusedShape {
     static constexpr int THREADS = TILE % 512 == 0 ? 512 : pass_shape_small_row(KB, 0).threads;
     static constexpr int IPT = TILE / THREADS;
     static constexpr int MIN_CTAS = pass_shape_small_row(KB, 0).min_ctas;
+    // keys per thread of the bucket sort after the MSD partition: buckets of
+    // up to THREADS * LIPT keys (2 and 4-byte keys 8192, 8-byte 7168, 16-byte
+    // 3072), sized so that two CTAs still fit an SM
+    static constexpr int LIPT = KB == 1 ? IPT : KB <= 4 ? 2 * IPT : KB == 8 ? 28 : 6;
 };
 
 // Predecessor tiles per lookback round trip for short arrays: all their tiles

@@ -88,6 +88,13 @@ std::atomic<int> g_short_fused{[] {
     const char* v = std::getenv("GBSORT_SHORT_FUSED");
     return (v && v[0] == '0') ? 0 : 1;
 }()};
+// Inside it, the MSD partition + per-CTA bucket sorts when every top-digit
+// bucket fits one CTA (fused_short.cuh): on unless GBSORT_SHORT_MSD=0 or
+// switched off (gbsort_set_short_msd).
+std::atomic<int> g_short_msd{[] {
+    const char* v = std::getenv("GBSORT_SHORT_MSD");
+    return (v && v[0] == '0') ? 0 : 1;
+}()};
 // Uniform-digit pass skipping: on unless GBSORT_PASS_SKIP=0 or switched off.
 std::atomic<int> g_pass_skip{[] {
     const char* v = std::getenv("GBSORT_PASS_SKIP");
@@ -274,7 +281,7 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     const bool small = n <= SMALL_N_MAX && !p.wide_status;
     p.pass = pass_entries(p.kb)[vi * 3 + (small ? 2 : p.wide_status ? 1 : 0)];
     // short keys-only arrays: one cooperative launch of the same pass shape
-    if (small && n <= FUSED_N_MAX && p.vb == 0 && g_short_fused.load(std::memory_order_relaxed))
+    if (small && n <= fused_n_max(p.kb) && p.vb == 0 && g_short_fused.load(std::memory_order_relaxed))
         p.fused = *fused_entry(p.kb);
     p.upsweep = *upsweep_entry(p.kb);
     const uint64_t tiles = (n + uint64_t(p.pass.tile) - 1) / uint64_t(p.pass.tile);
@@ -406,7 +413,13 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         return fp;
     };
 
-    cudaError_t e = cudaMemsetAsync(ctl, 0, plan.ctl.bytes, stream);
+    // the one-launch short sort runs when its kernel can be made resident
+    const bool fused =
+        plan.fused.fn != nullptr && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0;
+    // it starts from cleared lookback status words too: they follow the
+    // control block, and both are cleared by one memset
+    const size_t clear_bytes = fused ? plan.status_off + plan.status_bytes - plan.ctl_off : plan.ctl.bytes;
+    cudaError_t e = cudaMemsetAsync(ctl, 0, clear_bytes, stream);
     if (e != cudaSuccess) return fail("memset control block", e);
 
     HistParams hp{};
@@ -421,7 +434,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     hp.vals = copy ? vals_src : d_values;
     hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
     hp.val_bytes_total = plan.n * uint64_t(plan.vb);
-    if (plan.fused.fn != nullptr && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0) {
+    if (fused) {
         // Short array: the whole sort in one cooperative launch (every CTA
         // resident, or the launch fails; fused_short.cuh).
         FusedParams f{};
@@ -431,8 +444,13 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         f.fixup = fixup ? 1 : 0;
         f.barrier = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_off);
         f.barrier_gen = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_gen_off);
+        f.msd = g_short_msd.load(std::memory_order_relaxed);
         const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
-        const uint32_t grid = uint32_t(plan.num_tiles < fmax ? plan.num_tiles : fmax);
+        // one CTA per tile; when the MSD partition may apply, at least one
+        // per top-digit bucket, so that bucket sorts run side by side
+        uint64_t want = plan.num_tiles;
+        if (f.msd && plan.passes >= 2 && want < 256) want = 256;
+        const uint32_t grid = uint32_t(want < fmax ? want : fmax);
         void* args[] = {&f};
         if (timed) cudaEventRecord(ev[0], stream);
         e = cudaLaunchCooperativeKernel(plan.fused.fn, dim3(grid), dim3(plan.fused.threads), args, plan.fused.smem,
@@ -534,14 +552,14 @@ int check_args(int key_type, size_t value_bytes, void* d_keys, void* d_values, s
 // graph, if any, is destroyed; one still running is freed by CUDA when it
 // completes).  gbsort_graph_cache_clear() frees them all.
 struct GraphKey {
-    int device, key_type, desc, skip, fused;
+    int device, key_type, desc, skip, fused, msd;
     size_t vb;
     uint64_t n, wait_limit;
     const void *keys, *vals, *ws, *ksrc, *vsrc, *keys_b, *vals_b;
     cudaStream_t stream;
     auto tie() const {
-        return std::tie(device, key_type, desc, skip, fused, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc, keys_b,
-                        vals_b, stream);
+        return std::tie(device, key_type, desc, skip, fused, msd, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc,
+                        keys_b, vals_b, stream);
     }
     bool operator==(const GraphKey& o) const { return tie() == o.tie(); }
 };
@@ -579,6 +597,7 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
     k.desc = descending;
     k.skip = g_pass_skip.load(std::memory_order_relaxed);
     k.fused = plan.fused.fn != nullptr;
+    k.msd = g_short_msd.load(std::memory_order_relaxed);
     k.vb = size_t(plan.vb);
     k.n = plan.n;
     k.wait_limit = wait_limit_ns();
@@ -919,6 +938,8 @@ void gbsort_set_pass_skip(int enable) { g_pass_skip.store(enable ? 1 : 0, std::m
 int gbsort_get_pass_skip(void) { return g_pass_skip.load(std::memory_order_relaxed); }
 void gbsort_set_short_fused(int enable) { g_short_fused.store(enable ? 1 : 0, std::memory_order_relaxed); }
 int gbsort_get_short_fused(void) { return g_short_fused.load(std::memory_order_relaxed); }
+void gbsort_set_short_msd(int enable) { g_short_msd.store(enable ? 1 : 0, std::memory_order_relaxed); }
+int gbsort_get_short_msd(void) { return g_short_msd.load(std::memory_order_relaxed); }
 
 void gbsort_set_wait_limit_ns(uint64_t ns) { g_wait_limit_ns.store(ns, std::memory_order_relaxed); }
 uint64_t gbsort_get_wait_limit_ns(void) { return wait_limit_ns(); }
@@ -945,7 +966,9 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
     out->kernel_launches = uint32_t(plan.passes + 1 + ((gbsort_get_pass_skip() && (plan.passes & 1) == 0) ? 1 : 0));
     if (plan.fused.fn && sms > 0 && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0) {
         const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
-        out->pass_ctas = uint32_t(plan.num_tiles < fmax ? plan.num_tiles : fmax);
+        uint64_t want = plan.num_tiles;
+        if (g_short_msd.load(std::memory_order_relaxed) && plan.passes >= 2 && want < 256) want = 256;
+        out->pass_ctas = uint32_t(want < fmax ? want : fmax);
         out->hist_ctas = 0;  // counted by the same launch
         out->kernel_launches = 1;
     }

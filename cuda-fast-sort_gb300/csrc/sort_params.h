@@ -105,6 +105,7 @@ struct FusedParams {
     int fixup;              // run the fix-up phase
     uint32_t* barrier;      // grid barrier counter and generation, zeroed before the launch
     uint32_t* barrier_gen;
+    int msd;                // allow the MSD partition + bucket sorts
 };
 
 // Batched upsweep: one work item per chunk of one segment.

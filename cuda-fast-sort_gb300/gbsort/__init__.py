@@ -596,6 +596,20 @@ def get_short_fused() -> bool:
     return bool(f())
 
 
+def set_short_msd(enable: bool) -> None:
+    """MSD partition + per-CTA bucket sorts inside the one-launch short sort."""
+    f = lib().gbsort_set_short_msd
+    f.restype = None
+    f.argtypes = [ctypes.c_int]
+    f(int(enable))
+
+
+def get_short_msd() -> bool:
+    f = lib().gbsort_get_short_msd
+    f.restype = ctypes.c_int
+    return bool(f())
+
+
 def sort_copy(keys_in, keys_out, n: int, key_type, workspace, workspace_bytes: int, *, values_in=None,
               values_out=None, value_bytes: int = 0, descending: bool = False, stream=None) -> None:
     """Input-preserving sort (gbsort_sort_keys_copy / gbsort_sort_pairs_copy):

@@ -454,7 +454,8 @@ int gbsort_workspace_status(int key_type, size_t value_bytes, size_t n,
 void gbsort_set_pass_skip(int enable);
 int gbsort_get_pass_skip(void);
 
-/* One-launch sort of short keys-only arrays (n <= 2^21, no values; plain,
+/* One-launch sort of short keys-only arrays (n <= 2^21, 2^20 for 16-byte
+ * keys; no values; plain,
  * input-preserving and DoubleBuffer forms): the digit counts, every pass and
  * the pass-skip fix-up run in one cooperative launch with a grid barrier
  * (bounded wait, GBSORT_ERR_TIMEOUT) between them, instead of one launch per
@@ -464,6 +465,16 @@ int gbsort_get_pass_skip(void);
  * Results are identical either way. */
 void gbsort_set_short_fused(int enable);
 int gbsort_get_short_fused(void);
+
+/* Inside the one-launch short sort (keys of 2 bytes or more): when every
+ * bucket of the most significant digit fits one CTA (8192 keys of 2 or 4
+ * bytes, 5120 of 8, 2048 of 16), one pass partitions the keys by that digit
+ * and each CTA then sorts whole buckets in shared memory over the remaining
+ * digits — one grid-wide exchange instead of one per digit.  Otherwise (or
+ * when switched off: GBSORT_SHORT_MSD=0, gbsort_set_short_msd(0)) every
+ * digit takes a pass.  The stable sort's result either way. */
+void gbsort_set_short_msd(int enable);
+int gbsort_get_short_msd(void);
 
 /* Graph replay of repeated calls (default on; GBSORT_GRAPH_CACHE=0 turns it
  * off at load).  The second call of gbsort_sort_keys / _pairs / _copy with

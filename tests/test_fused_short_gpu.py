@@ -11,7 +11,10 @@ this path (it is the default).  Here:
   - the grid barrier's bounded wait runs out on a barrier nothing completes
     (GBSORT_ERR_TIMEOUT) and the context stays usable;
   - a one-launch sort whose waits all run out (1 ns limit) reports
-    GBSORT_ERR_TIMEOUT, and the next sort is correct.
+    GBSORT_ERR_TIMEOUT, and the next sort is correct;
+  - the MSD partition + bucket sorts give the same bytes as every digit
+    taking a pass, and a top-digit bucket too big for one CTA falls back to
+    the passes (both against the oracle).
 """
 
 import numpy as np
@@ -113,3 +116,33 @@ def test_one_launch_reports_timed_out_waits(gb, cuda, oracle, fused_default):
     cuda.cuda.synchronize()
     assert gb.workspace_status("u32", n, ws) == gb.OK
     assert _eq(from_dev(d, raw), oracle.sort("u32", raw, False))
+
+
+@pytest.fixture
+def msd_default(gb):
+    old = gb.get_short_msd()
+    yield
+    gb.set_short_msd(old)
+
+
+@pytest.mark.parametrize("kt", ["u16", "i32", "f32", "u64", "f64", "u128", "f128"])
+@pytest.mark.parametrize("desc", [False, True])
+def test_msd_buckets_equal_digit_passes(gb, cuda, oracle, fused_default, msd_default, kt, desc):
+    raw = raw_keys(kt, 200_003, seed=21 + len(kt))  # buckets of ~800 keys: the partition applies
+    gb.set_short_msd(True)
+    part = gpu_sort(gb, cuda, kt, raw, desc)
+    gb.set_short_msd(False)
+    passes = gpu_sort(gb, cuda, kt, raw, desc)
+    assert _eq(part, passes)
+    assert _eq(part, oracle.sort(kt, raw, desc))
+
+
+@pytest.mark.parametrize("n", [1 << 20, (1 << 21) - 3])
+def test_msd_big_bucket_falls_back(gb, cuda, oracle, fused_default, msd_default, n):
+    raw = raw_keys("u32", n, seed=9)
+    raw[::5] = (raw[::5] & np.uint32(0x00FFFFFF)) | np.uint32(0x55000000)  # one bucket of n/5 keys
+    gb.set_short_msd(True)
+    got = gpu_sort(gb, cuda, "u32", raw)
+    assert _eq(got, oracle.sort("u32", raw, False))
+    gb.set_short_msd(False)
+    assert _eq(gpu_sort(gb, cuda, "u32", raw), got)
