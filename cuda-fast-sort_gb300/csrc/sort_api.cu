@@ -468,8 +468,10 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
             }
             return GBSORT_OK;
         }
-        if (e != cudaErrorCooperativeLaunchTooLarge) return fail("one-launch sort", e);
-        cudaGetLastError();  // the grid cannot be resident at once here: the multi-launch path follows
+        // the launch was refused (e.g. the grid cannot be resident at once
+        // here): the separate launches follow; an error that outlives the
+        // refusal surfaces at their first launch
+        cudaGetLastError();
     }
     const uint32_t hist_ctas = upsweep_ctas(plan.n, plan.kb);
     {
