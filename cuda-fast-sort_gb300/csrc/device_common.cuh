@@ -388,19 +388,40 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 
 // Grid-wide barrier of a cooperative launch (every CTA resident at once).
-// counter and gen start at 0 (gen in another 128-byte line, so the waiting
-// CTAs' polls do not queue behind the arrivals' atomics).  The k-th barrier
-// of the launch (k = 1, 2, ...): thread 0 of each CTA arrives with a release
-// (atomicAdd on counter); the CTA that brings counter to k * gridDim.x
-// publishes gen = k; the others poll gen with acquire loads, bounded by
-// limit_ns: a wait that runs out records ERRBIT_TIMEOUT and the barrier
-// returns false on every thread of that CTA, so the caller can leave
-// instead of hanging.
+// counter and gen start at 0.  The k-th barrier of the launch (k = 1, 2,
+// ...): thread 0 of each CTA fences and adds 1 to counter, then polls
+// counter with acquire loads until it reaches k * gridDim.x (by default), or
+// — with GBSORT_BARRIER_POLL_COUNTER 0 — the CTA that brings counter there
+// publishes gen = k (another 128-byte line, away from the arrivals'
+// atomics) and the others poll gen.  Either wait is bounded by limit_ns: a
+// wait that runs out records ERRBIT_TIMEOUT and the barrier returns false
+// on every thread of that CTA, so the caller can leave instead of hanging.
+// Polling the counter saves the generation word's extra round trip: 2^20
+// u32 keys in one launch 24.3 vs 25.2 us, 2^19 u128 22.4 vs 24.1.
+// Nonzero: the ns each poll of the counter sleeps before the next.
+#ifndef GBSORT_BARRIER_POLL_COUNTER
+#define GBSORT_BARRIER_POLL_COUNTER 32
+#endif
 __device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t* gen, uint32_t k, uint64_t limit_ns,
                                              uint32_t* err) {
     __syncthreads();
     int ok = 1;
-    if (threadIdx.x == 0) {
+    if (GBSORT_BARRIER_POLL_COUNTER && threadIdx.x == 0) {
+        // every CTA polls the counter itself: no generation word to publish
+        __threadfence();
+        asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
+        const uint32_t target = k * gridDim.x;
+        const uint64_t t0 = global_timer_ns();
+        while (ld_acquire(counter) < target) {
+            if (global_timer_ns() - t0 > limit_ns) {
+                atomicOr(err, ERRBIT_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            __nanosleep(GBSORT_BARRIER_POLL_COUNTER);
+        }
+        __threadfence();
+    } else if (threadIdx.x == 0) {
         __threadfence();
         const uint32_t arrived = atomicAdd(counter, 1u) + 1u;
         if (arrived == k * gridDim.x) {

@@ -253,6 +253,175 @@ __device__ __forceinline__ void cta_bucket_sort(const typename KeyBits<KB>::U* s
     __syncthreads();  // the buffers and counters are free for the next bucket
 }
 
+// Exclusive scan of one value per thread over the whole CTA (warp_tmp: one
+// word per warp).  Every thread must call it.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_scan_all(uint32_t x, uint32_t* warp_tmp) {
+    constexpr int WARPS = THREADS / 32;
+    static_assert(WARPS <= 32, "one warp scans the warp totals");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) warp_tmp[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = (lane < WARPS) ? warp_tmp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < WARPS; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < WARPS) warp_tmp[lane] = t;  // inclusive warp totals
+    }
+    __syncthreads();
+    return (warp > 0 ? warp_tmp[warp - 1] : 0u) + v - x;
+}
+
+__host__ __device__ constexpr int floor_log2(int x) { return x <= 1 ? 0 : 1 + floor_log2(x / 2); }
+
+// Largest sub-bucket the split sort ranks by comparison (a key compares
+// itself with every key of its sub-bucket).
+#ifndef GBSORT_SPLIT_MAX
+#define GBSORT_SPLIT_MAX 32
+#endif
+// 0: every bucket takes the per-digit bucket sort.
+#ifndef GBSORT_BUCKET_SPLIT
+#define GBSORT_BUCKET_SPLIT 1
+#endif
+
+// One bucket (cnt <= THREADS * LIPT twiddled keys that share their top digit,
+// already in registers: key u of this thread is the bucket's key
+// u * THREADS + tid) sorted by splitting it, keys only.  One counting pass
+// over the next RB bits below the top digit (2^RB sub-buckets) moves every
+// key into its sub-bucket with a shared-memory atomic, in no particular
+// order: equal twiddled keys are equal bytes, so once the keys are in
+// order, the order among equal keys cannot show.  A sub-bucket then holds
+// the keys of one value of the top 8 + RB bits, cnt / 2^RB on average (about
+// half a key at 2^20 keys), and a key's place in it is the number of the
+// sub-bucket's other keys below it (equal keys ordered by where the
+// counting pass put them), written straight to dst.  Where nothing is left
+// below the RB bits (2-byte keys), the counting pass alone sorts.  So the
+// bucket costs one counting pass and a comparison or two per key instead
+// of a ranked pass per remaining digit.  Returns false, having written
+// nothing outside shared memory, when a sub-bucket holds more than
+// GBSORT_SPLIT_MAX keys (repeated keys, or keys that share those bits): the
+// per-digit bucket sort takes those.
+// One word per sub-bucket at ctr (2^RB <= CTR_WORDS words, left zeroed;
+// here the warp histograms and the match words after them): the count,
+// then start << 16 | cursor (cnt < 2^16).  Sub-bucket b lives in word
+// b ^ ((b >> 5) & 31), which puts the scan's runs of 2^k consecutive
+// sub-buckets per thread on distinct banks.
+__host__ __device__ constexpr int split_slot(int b) { return b ^ ((b >> 5) & 31); }
+
+template <int KB, int THREADS, int LIPT, int CTR_WORDS>
+__device__ __forceinline__ bool cta_bucket_split(const typename KeyBits<KB>::U (&keys)[LIPT],
+                                                 typename KeyBits<KB>::U* dst, uint32_t cnt, uint8_t* buf,
+                                                 uint32_t* ctr, uint32_t* scan, uint32_t* largest, int kind,
+                                                 int desc) {
+    using U = typename KeyBits<KB>::U;
+    constexpr int BELOW = 8 * (KB - 1);  // key bits below the bucket's digit
+    constexpr int RB_CAP = floor_log2(CTR_WORDS);
+    constexpr int RB = RB_CAP < BELOW ? RB_CAP : BELOW;
+    constexpr int BINS = 1 << RB;
+    static_assert(BINS >= 32 && BINS <= CTR_WORDS, "sub-bucket words");
+    static_assert(THREADS * LIPT < 65536, "16-bit starts and cursors");
+    constexpr int SHIFT = BELOW - RB;  // key bits left to compare inside a sub-bucket
+    constexpr int PER = (BINS + THREADS - 1) / THREADS;
+    static_assert((PER & (PER - 1)) == 0 && PER <= 32, "runs of 2^k sub-buckets per thread");
+    const int tid = threadIdx.x;
+    U* sk = reinterpret_cast<U*>(buf);
+    auto slot = [](U k) { return split_slot(int(uint32_t(k >> SHIFT) & uint32_t(BINS - 1))); };
+    auto valid = [&](int u) { return uint32_t(u * THREADS + tid) < cnt; };
+    for (int i = tid; i < BINS; i += THREADS) ctr[i] = 0u;
+    if (tid == 0) *largest = 0u;
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < LIPT; ++u)
+        if (valid(u)) atomicAdd(&ctr[slot(keys[u])], 1u);
+    __syncthreads();
+    uint32_t c[PER], sum = 0, big = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int b = tid * PER + i;
+        c[i] = (b < BINS) ? ctr[split_slot(b)] : 0u;
+        sum += c[i];
+        big = max(big, c[i]);
+    }
+    uint32_t run = block_exclusive_scan_all<THREADS>(sum, scan);
+    big = __reduce_max_sync(0xffffffffu, big);
+    if ((tid & 31) == 0 && big > uint32_t(GBSORT_SPLIT_MAX)) atomicMax(largest, big);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int b = tid * PER + i;
+        if (b < BINS) ctr[split_slot(b)] = run << 16 | run;
+        run += c[i];
+    }
+    __syncthreads();
+    if (SHIFT > 0 && *largest > uint32_t(GBSORT_SPLIT_MAX)) {
+        for (int i = tid; i < BINS; i += THREADS) ctr[i] = 0u;
+        __syncthreads();
+        return false;
+    }
+#pragma unroll
+    for (int u = 0; u < LIPT; ++u)
+        if (valid(u)) sk[atomicAdd(&ctr[slot(keys[u])], 1u) & 0xffffu] = keys[u];
+    __syncthreads();
+    if constexpr (SHIFT > 0) {
+        // the key at place i goes to its sub-bucket's start plus the
+        // sub-bucket's other keys below it: a place near i, so a warp's
+        // stores stay nearly coalesced; CH places per thread compared at once
+#ifdef GBSORT_SPLIT_CH
+        constexpr int CH = GBSORT_SPLIT_CH;
+#else
+        constexpr int CH = 1;
+#endif
+        for (uint32_t i0 = tid; i0 < cnt; i0 += CH * THREADS) {
+            U k[CH];
+            uint32_t st[CH], others[CH], below[CH], most = 0;
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const uint32_t i = i0 + u * THREADS;
+                k[u] = (i < cnt) ? sk[i] : U(0);
+            }
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const uint32_t i = i0 + u * THREADS;
+                const uint32_t w = (i < cnt) ? ctr[slot(k[u])] : 0u;
+                st[u] = w >> 16;
+                others[u] = (i < cnt) ? (w & 0xffffu) - st[u] - 1u : 0u;
+                below[u] = 0;
+                most = max(most, others[u]);
+            }
+            for (uint32_t j = 0; j < most; ++j) {
+#pragma unroll
+                for (int u = 0; u < CH; ++u) {
+                    if (j < others[u]) {
+                        const uint32_t i = i0 + u * THREADS;
+                        const uint32_t q = st[u] + j + uint32_t(st[u] + j >= i);  // every place but i
+                        const U o = sk[q];
+                        below[u] += uint32_t(o < k[u] || (o == k[u] && q < i));
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const uint32_t i = i0 + u * THREADS;
+                if (i < cnt) dst[st[u] + below[u]] = twiddle_out<U>(k[u], kind, desc);
+            }
+        }
+    } else {
+        for (uint32_t i = tid; i < cnt; i += THREADS) dst[i] = twiddle_out<U>(sk[i], kind, desc);
+    }
+    __syncthreads();
+    for (int i = tid; i < BINS; i += THREADS) ctr[i] = 0u;
+    __syncthreads();
+    return true;
+}
+
 template <int KB, int THREADS, int IPT, int LIPT, int MIN_CTAS>
 __global__ void __launch_bounds__(THREADS, MIN_CTAS) fused_short_kernel(FusedParams f) {
     using U = typename KeyBits<KB>::U;
@@ -388,60 +557,121 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) fused_short_kernel(FusedPar
             tile_back(q, t, kout, tw_store, keys, st, gex + q * 256);
         }
     };
-    // The buckets of the top digit (offsets `top`), each sorted by one CTA
-    // from the partition `part` home.
-    auto bucket_sorts = [&](const U* part, U* home, const uint32_t* top) {
-        for (uint32_t b = blockIdx.x; b < 256; b += gridDim.x) {
-            const uint32_t begin = top[b], end = (b < 255) ? top[b + 1] : n;
-            if (end > begin)  // the top digit is the bucket's: digits below it only
-                cta_bucket_sort<KB, THREADS, LIPT>(part + begin, home + begin, end - begin, G::P - 1, smem, whist,
-                                                   mscratch, scan, kind, desc);
+    // MSD partition of one tile (keys of 2 bytes or more): its keys go to
+    // the regions of their top digit (f.regions: 256 regions of
+    // f.region_cap keys), where the tile claims its places with one atomic
+    // per digit on the region's fill count (f.fill) — no tile waits for
+    // another, and the order inside a region is arbitrary (keys only: equal
+    // twiddled keys are equal bytes, and the bucket sorts need no order).
+    // A region that would overflow is not written past its end and raises
+    // f.overflow.
+    auto partition_tile = [&](uint32_t t, const U* kin, U* regions, uint32_t cap) {
+        constexpr int q = G::P - 1;
+        uint32_t* gbase = gex;  // [256] the tile's first place in each region
+        const uint64_t base = uint64_t(t) * G::TILE;
+        const uint32_t cnt = (n - base) < uint64_t(G::TILE) ? uint32_t(n - base) : uint32_t(G::TILE);
+        U keys[IPT];
+        uint32_t slot[IPT];
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            const uint32_t j = uint32_t(u * THREADS + tid);
+            keys[u] = (j < cnt) ? twiddle_in<U>(kin[base + j], kind, desc) : U(0);
         }
+        if (tid < 256) binb[tid] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < IPT; ++u)
+            if (uint32_t(u * THREADS + tid) < cnt) slot[u] = atomicAdd(&binb[digit_of(keys[u], q)], 1u);
+        __syncthreads();
+        uint32_t c = 0, g = 0;
+        if (tid < 256) {
+            c = binb[tid];
+            if (c) {
+                g = atomicAdd(f.fill + tid, c);
+                if (g + c > cap) atomicOr(f.overflow, 1u);
+            }
+        }
+        const uint32_t ex = block_exclusive_scan_256<uint32_t>(c, scan, nullptr);
+        if (tid < 256) {
+            binb[tid] = ex;
+            gbase[tid] = g;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < IPT; ++u)
+            if (uint32_t(u * THREADS + tid) < cnt) stage[binb[digit_of(keys[u], q)] + slot[u]] = keys[u];
+        __syncthreads();
+        // coalesced runs, one per digit
+        for (uint32_t j = tid; j < cnt; j += THREADS) {
+            const U k = stage[j];
+            const uint32_t d = digit_of(k, q);
+            const uint32_t pos = gbase[d] + (j - binb[d]);
+            if (pos < cap) regions[size_t(d) * cap + pos] = k;
+        }
+        __syncthreads();  // the stage and the digit words are free for the next tile
     };
 
-    const U* msd_src = static_cast<const U*>(p.copy_keys_in ? p.copy_keys_in : p.keys_a);
-    U* msd_part = static_cast<U*>(p.keys_b);
-    U* msd_home = static_cast<U*>(p.keys_a);
-    if (tid == 0) {
-        misc[0] = 0u;
-        misc[1] = 0u;
-    }
-
-    // MSD first (keys of 2 bytes or more, at most one tile per CTA): the
-    // partition pass takes the top digit's global counts from its own group
-    // sums (every CTA adds all of them up), so no counting phase and no
-    // barrier precede it.  The status words start cleared (the host clears
-    // them with the control block).  If a bucket is too big for one CTA,
-    // nothing has moved yet: once every CTA has read the status words, the
-    // counting phase below clears them and every digit takes a pass.
-    if (G::P >= 2 && f.msd && T <= gridDim.x) {
-        for (int i = tid; i < G::WARPS * 256; i += THREADS) mscratch[i] = 0u;
-        __syncthreads();
-        constexpr int q = G::P - 1;
-        const uint32_t t = blockIdx.x;
-        const bool has_tile = t < T;  // CTA-uniform
-        U keys[IPT];
-        TileState st{};
-        if (has_tile) tile_front(q, t, msd_src, true, keys, st);
-        uint32_t* top = gex + q * 256;
-        uint32_t tot = 0;
-        if (tid < 256)
-            tot = sum_published<Codec>(agg + tid, (T + SHORT_GROUP - 1) / SHORT_GROUP, uint32_t(q), limit, err);
-        const uint32_t ex = block_exclusive_scan_256<uint32_t>(tot, scan, nullptr);
-        if (tid < 256) {
-            top[tid] = ex;
-            atomicMax(&misc[1], tot);
-        }
-        __syncthreads();
-        if (misc[1] <= uint32_t(G::LOCAL_TILE)) {
-            if (has_tile) tile_back(q, t, msd_part, false, keys, st, top);
+    // MSD first (keys of 2 bytes or more, when the plan has regions): the
+    // partition, one grid barrier, then each CTA sorts whole buckets from
+    // their regions into their places in the result (the result is home: no
+    // fix-up).  After an overflow every CTA goes on to the per-digit passes
+    // below, which start from the untouched input.
+    if (tid == 0) misc[0] = 0u;
+    if constexpr (G::P >= 2) {
+        if (f.msd) {
+            for (int i = tid; i < G::WARPS * 256; i += THREADS) mscratch[i] = 0u;  // the match words start zeroed
+            U* regions = static_cast<U*>(f.regions);
+            const uint32_t cap = f.region_cap;
+            const U* src = static_cast<const U*>(p.copy_keys_in ? p.copy_keys_in : p.keys_a);
+            for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) partition_tile(t, src, regions, cap);
             if (!grid_barrier(f.barrier, f.barrier_gen, ++phase, limit, err)) return;
             if (ld_relaxed(err) != 0u) return;
-            bucket_sorts(msd_part, msd_home, top);
-            return;  // the result is home: no fix-up
+            if (ld_relaxed(f.overflow) == 0u) {
+                // every bucket's size and place in the result; the keys of this
+                // CTA's first bucket are loaded meanwhile (every place of its
+                // region: those past its size are never used)
+                uint32_t* top = gex + 256;
+                U keys[LIPT];
+                const U* first = regions + size_t(blockIdx.x) * cap;
+#pragma unroll
+                for (int u = 0; u < LIPT; ++u) {
+                    const uint32_t j = uint32_t(u * THREADS + tid);
+                    keys[u] = (blockIdx.x < 256 && j < cap) ? first[j] : U(0);
+                }
+                const uint32_t fc = (tid < 256) ? ld_relaxed(f.fill + tid) : 0u;
+                const uint32_t ex = block_exclusive_scan_256<uint32_t>(fc, scan, nullptr);
+                if (tid < 256) {
+                    binb[tid] = fc;
+                    top[tid] = ex;
+                }
+                __syncthreads();
+                U* home = static_cast<U*>(p.keys_a);
+                // the top digit is the bucket's: digits below it only; the split
+                // first, the per-digit sort where a sub-bucket is too big
+                auto sort_bucket = [&](uint32_t b, const U (&keys)[LIPT]) {
+                    const uint32_t c = binb[b];
+                    if (c == 0) return;
+                    U* to = home + top[b];
+                    if (GBSORT_BUCKET_SPLIT && cta_bucket_split<KB, THREADS, LIPT, 2 * G::WARPS * 256>(
+                                                   keys, to, c, smem, whist, scan, misc + 2, kind, desc))
+                        return;
+                    cta_bucket_sort<KB, THREADS, LIPT>(regions + size_t(b) * cap, to, c, G::P - 1, smem, whist,
+                                                       mscratch, scan, kind, desc);
+                };
+                if (blockIdx.x < 256) sort_bucket(blockIdx.x, keys);
+                for (uint32_t b = blockIdx.x + gridDim.x; b < 256; b += gridDim.x) {
+                    U more[LIPT];
+                    const U* from = regions + size_t(b) * cap;
+#pragma unroll
+                    for (int u = 0; u < LIPT; ++u) {
+                        const uint32_t j = uint32_t(u * THREADS + tid);
+                        more[u] = (j < binb[b]) ? from[j] : U(0);
+                    }
+                    sort_bucket(b, more);
+                }
+                return;
+            }
         }
-        if (!grid_barrier(f.barrier, f.barrier_gen, ++phase, limit, err)) return;
-        if (tid == 0) misc[1] = 0u;
     }
 
     fused_counts<KB, THREADS>(f.hist, smem, G::COUNT_BYTES);
@@ -469,36 +699,12 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) fused_short_kernel(FusedPar
 #pragma unroll
         for (int j = 0; j < 8; ++j) gex[q * 256 + lane * 8 + j] = c[j] + incl - run;
         if (__any_sync(0xffffffffu, uni) && lane == 0) atomicOr(&misc[0], 1u << q);
-        if (q == G::P - 1) {  // the largest bucket of the top digit
-            uint32_t mx = 0;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const uint32_t next = (j < 7) ? c[j + 1] : run;
-                mx = max(mx, next - c[j]);
-            }
-            mx = __reduce_max_sync(0xffffffffu, mx);
-            if (lane == 0) misc[1] = mx;
-        }
     }
     __syncthreads();
     const uint32_t all = (G::P >= 32) ? 0xffffffffu : ((1u << G::P) - 1u);
     const uint32_t uniform = p.skip ? (misc[0] & all) : 0u;
     const int total = __popc(~uniform & all);
     if (p.executed && blockIdx.x == 0 && tid == 0) *p.executed = 0x80000000u | uint32_t(total);
-
-    // MSD partition (keys of 2 bytes or more), after the counts of every
-    // digit: when every bucket of the top digit fits one CTA's local sort,
-    // one pass on the top digit moves the keys into their buckets (caller's
-    // buffer or input -> alternate buffer, twiddled), and each CTA then sorts
-    // whole buckets in shared memory over the remaining digits and writes
-    // them home: one grid-wide exchange instead of one per digit.
-    if (G::P >= 2 && f.msd && misc[1] <= uint32_t(G::LOCAL_TILE)) {
-        run_pass(G::P - 1, msd_src, msd_part, true, false);
-        if (!grid_barrier(f.barrier, f.barrier_gen, ++phase, limit, err)) return;
-        if (ld_relaxed(err) != 0u) return;
-        bucket_sorts(msd_part, msd_home, gex + (G::P - 1) * 256);
-        return;  // the result is home: no fix-up
-    }
 
     int before = 0;  // executed passes so far
     for (int q = 0; q < G::P; ++q) {

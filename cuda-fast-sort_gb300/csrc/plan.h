@@ -25,6 +25,8 @@ struct CtlLayout {
     size_t exec_off = 0;
     size_t barrier_off = 0;      // grid barrier counter of the one-launch short sort
     size_t barrier_gen_off = 0;  // its generation word (another 128-byte line)
+    size_t fill_off = 0;         // [256] fill counts of its MSD regions
+    size_t overflow_off = 0;     // its region overflow flag
     size_t bytes = 0;
     static CtlLayout make(int passes) {
         CtlLayout c;
@@ -34,7 +36,9 @@ struct CtlLayout {
         c.exec_off = c.err_off + 4;
         c.barrier_off = c.exec_off + 4;
         c.barrier_gen_off = align_up(c.barrier_off + 4, 128);
-        c.bytes = align_up(c.barrier_gen_off + 4, 256);
+        c.fill_off = align_up(c.barrier_gen_off + 4, 128);
+        c.overflow_off = c.fill_off + 256 * 4;
+        c.bytes = align_up(c.overflow_off + 4, 256);
         return c;
     }
 };
@@ -59,6 +63,9 @@ struct Plan {
     size_t ctl_off = 0;
     size_t status_off = 0;
     size_t status_bytes = 0;
+    // the one-launch sort's MSD regions: 256 x msd_cap keys (msd_cap 0: none)
+    size_t regions_off = 0;
+    uint32_t msd_cap = 0;
     size_t total_bytes = 0;
     CtlLayout ctl{};
 };

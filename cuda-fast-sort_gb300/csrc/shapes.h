@@ -6,6 +6,8 @@
 // holds keys, values and ranks without spilling.
 #pragma once
 
+#include <cmath>
+
 #include <cstdint>
 
 namespace gbsort {
@@ -77,6 +79,26 @@ struct FusedShape {
     // 3072), sized so that two CTAs still fit an SM
     static constexpr int LIPT = KB == 1 ? IPT : KB <= 4 ? 2 * IPT : KB == 8 ? 28 : 6;
 };
+
+// Keys per bucket the one-launch sort's CTA sorts in shared memory.
+constexpr int fused_local_tile(int kb) {
+    return kb == 1    ? FusedShape<1>::THREADS * FusedShape<1>::LIPT
+           : kb == 2  ? FusedShape<2>::THREADS * FusedShape<2>::LIPT
+           : kb == 4  ? FusedShape<4>::THREADS * FusedShape<4>::LIPT
+           : kb == 8  ? FusedShape<8>::THREADS * FusedShape<8>::LIPT
+                      : FusedShape<16>::THREADS * FusedShape<16>::LIPT;
+}
+
+// Keys per MSD region of the one-launch sort (one region per top digit):
+// the mean bucket n/256 plus four of its standard deviations plus 64,
+// rounded up to 32 (uniform top digits overflow a region about once in
+// 10^4 sorts at 2^20 keys, and then the sort takes the per-digit passes);
+// 0 where that exceeds a CTA's local sort.
+inline uint32_t msd_region_cap(int kb, uint64_t n) {
+    const double mean = double((n + 255) / 256);
+    const uint64_t cap = (uint64_t(mean + 4.0 * std::sqrt(mean) + 64.0) + 31) & ~uint64_t(31);
+    return cap <= uint64_t(fused_local_tile(kb)) ? uint32_t(cap) : 0u;
+}
 
 // Predecessor tiles per lookback round trip for short arrays: all their tiles
 // are in flight at once, so the known-prefix frontier moves a window per L2

@@ -300,6 +300,15 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
     // size query does not depend on which short path runs
     p.status_bytes = small ? short_status_words(p.num_tiles) * 4 : size_t(p.num_tiles) * 256 * (p.wide_status ? 8 : 4);
     off = align_up(off + p.status_bytes, 256);
+    // its MSD regions (keys-only arrays of 2-byte keys or wider), sized
+    // whether or not that path is switched on, for the same reason
+    if (small && n <= fused_n_max(p.kb) && p.vb == 0 && p.kb >= 2) {
+        p.msd_cap = msd_region_cap(p.kb, n);
+        if (p.msd_cap) {
+            p.regions_off = off;
+            off = align_up(off + size_t(256) * p.msd_cap * kb, 256);
+        }
+    }
     p.total_bytes = off;
     *plan = p;
     return GBSORT_OK;
@@ -444,12 +453,16 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         f.fixup = fixup ? 1 : 0;
         f.barrier = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_off);
         f.barrier_gen = reinterpret_cast<uint32_t*>(ctl + plan.ctl.barrier_gen_off);
-        f.msd = g_short_msd.load(std::memory_order_relaxed);
+        f.msd = (g_short_msd.load(std::memory_order_relaxed) && plan.msd_cap) ? 1 : 0;
+        f.regions = ws + plan.regions_off - ws_base;
+        f.region_cap = plan.msd_cap;
+        f.fill = reinterpret_cast<uint32_t*>(ctl + plan.ctl.fill_off);
+        f.overflow = reinterpret_cast<uint32_t*>(ctl + plan.ctl.overflow_off);
         const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
         // one CTA per tile; when the MSD partition may apply, at least one
         // per top-digit bucket, so that bucket sorts run side by side
         uint64_t want = plan.num_tiles;
-        if (f.msd && plan.passes >= 2 && want < 256) want = 256;
+        if (f.msd && want < 256) want = 256;
         const uint32_t grid = uint32_t(want < fmax ? want : fmax);
         void* args[] = {&f};
         if (timed) cudaEventRecord(ev[0], stream);
@@ -969,7 +982,7 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
     if (plan.fused.fn && sms > 0 && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0) {
         const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
         uint64_t want = plan.num_tiles;
-        if (g_short_msd.load(std::memory_order_relaxed) && plan.passes >= 2 && want < 256) want = 256;
+        if (g_short_msd.load(std::memory_order_relaxed) && plan.msd_cap && want < 256) want = 256;
         out->pass_ctas = uint32_t(want < fmax ? want : fmax);
         out->hist_ctas = 0;  // counted by the same launch
         out->kernel_launches = 1;

@@ -105,7 +105,11 @@ struct FusedParams {
     int fixup;              // run the fix-up phase
     uint32_t* barrier;      // grid barrier counter and generation, zeroed before the launch
     uint32_t* barrier_gen;
-    int msd;                // allow the MSD partition + bucket sorts
+    int msd;                // MSD partition into the regions + bucket sorts (needs regions)
+    void* regions;          // 256 regions of region_cap keys (workspace), one per top digit
+    uint32_t region_cap;
+    uint32_t* fill;         // [256] keys claimed in each region, zeroed before the launch
+    uint32_t* overflow;     // nonzero: a region overflowed (zeroed before the launch)
 };
 
 // Batched upsweep: one work item per chunk of one segment.

@@ -14,13 +14,17 @@ this path (it is the default).  Here:
     GBSORT_ERR_TIMEOUT, and the next sort is correct;
   - the MSD partition + bucket sorts give the same bytes as every digit
     taking a pass, and a top-digit bucket too big for one CTA falls back to
-    the passes (both against the oracle).
+    the passes (both against the oracle);
+  - the bucket split (a counting pass on the bits below the top digit, then
+    a comparison rank inside sub-buckets) beside buckets whose sub-buckets
+    are too big for it (bits below the top digit that coincide, keys
+    repeated a few or many times), against the oracle.
 """
 
 import numpy as np
 import pytest
 
-from _oracle import KEY_TYPES, raw_keys
+from _oracle import KEY_BYTES, KEY_TYPES, raw_keys
 from gpu_util import gpu_sort, from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
@@ -146,3 +150,43 @@ def test_msd_big_bucket_falls_back(gb, cuda, oracle, fused_default, msd_default,
     assert _eq(got, oracle.sort("u32", raw, False))
     gb.set_short_msd(False)
     assert _eq(gpu_sort(gb, cuda, "u32", raw), got)
+
+
+def _coincide_below_top(kt, raw):
+    """The keys whose top bit is set get one value for every bit between the
+    top byte and the lowest byte: their buckets have a single sub-bucket."""
+    out = raw.copy()
+    kb = KEY_BYTES[kt]
+    if kb == 16:
+        h = out.view(np.uint64).reshape(-1, 2)  # little-endian: column 1 holds the top byte
+        m = (h[:, 1] >> np.uint64(63)) == 1
+        h[m, 1] = (h[m, 1] & np.uint64(0xFF00000000000000)) | np.uint64(0x00ABCDEF12345678)
+        h[m, 0] &= np.uint64(0xFF)
+        return out
+    keep, const = {4: (0xFF0000FF, 0x00ABCD00), 8: (0xFF000000000000FF, 0x00ABCDEF12345600)}[kb]
+    t = out.dtype.type
+    m = (out >> t(8 * kb - 1)) == 1
+    out[m] = (out[m] & t(keep)) | t(const)
+    return out
+
+
+def _repeated(raw, distinct, seed):
+    rng = np.random.default_rng(seed)
+    return np.ascontiguousarray(raw[:distinct][rng.integers(0, distinct, raw.shape[0])])
+
+
+@pytest.mark.parametrize("kt", ["u32", "f32", "u64", "i64", "u128"])
+@pytest.mark.parametrize("shape", ["coincide", "repeat8", "repeat3000"])
+@pytest.mark.parametrize("desc", [False, True])
+def test_bucket_split_and_its_fallback(gb, cuda, oracle, fused_default, msd_default, kt, shape, desc):
+    n = 1 << 19 if kt == "u128" else 1 << 20
+    raw = raw_keys(kt, n, seed=41 + len(kt))
+    if shape == "coincide":
+        raw = _coincide_below_top(kt, raw)
+    else:  # about 8 copies of each key: sub-buckets with ties; 3000 keys: too big
+        raw = _repeated(raw, n // 8 if shape == "repeat8" else 3000, seed=n)
+    gb.set_short_msd(True)
+    got = gpu_sort(gb, cuda, kt, raw, desc)
+    assert _eq(got, oracle.sort(kt, raw, desc))
+    gb.set_short_msd(False)
+    assert _eq(gpu_sort(gb, cuda, kt, raw, desc), got)
