@@ -7,7 +7,26 @@
 // (digit offsets, uniform-pass check, tile claim, tile copy, lookback walk,
 // next claim, kernel boundary) around a few microseconds of ranking.  Here
 // one cooperative launch (every CTA resident at once, or the launch fails)
-// runs
+// sorts it, with a grid barrier between phases whose wait is bounded like
+// the lookback's (GBSORT_ERR_TIMEOUT, then every CTA leaves).
+//
+// Keys of 2 bytes or more, most significant digit first (keys only, so
+// equal twiddled keys are equal bytes and no step needs a stable order):
+//   partition: each tile counts its keys per top digit with shared-memory
+//            atomics, claims its places in the 256 fixed-capacity regions
+//            of the workspace (one per top digit) with one global atomic
+//            per digit, and writes its keys there as coalesced runs — no
+//            tile waits for another;
+//   one grid barrier;
+//   buckets: each CTA sorts whole top-digit buckets in shared memory (a
+//            counting pass on the next 12-13 bits, then a comparison rank
+//            inside the tiny sub-buckets; or, where a sub-bucket is too big,
+//            one ranked pass per remaining digit) and writes them to their
+//            places in the result.
+// A region that would overflow (skewed top digits) sends every CTA, after
+// the barrier, to the per-digit flow below, from the untouched input.
+//
+// Per-digit flow (1-byte keys, and the fallback):
 //   phase 0: every pass's digit counts from one read of the keys (plus the
 //            status clear and, for odd pass counts, the mirror);
 //   then, once per CTA, every pass's exclusive digit offsets and the mask of
@@ -20,13 +39,12 @@
 //            group of 16 publishes the group's sum, and a tile adds the sums
 //            of the groups before its own plus its own group's earlier
 //            counts — a fixed few round trips however many tiles;
-//   the parity fix-up copy when skipped passes leave the result elsewhere;
-// with a grid barrier between the phases whose wait is bounded like the
-// lookback's (GBSORT_ERR_TIMEOUT, then every CTA leaves).
-// The rank is the multi-launch pass's: warp histograms, early publication,
-// per-column warp match (shared-memory OR) + popc + one counter atomic per
-// digit group, staging at rank in shared memory (radix_kernel.cuh:118-294,
-// ranker.cuh:61-170, scatter.cuh:159-202 of the reference).
+//   the parity fix-up copy when skipped passes leave the result elsewhere.
+// The per-digit rank is the multi-launch pass's: warp histograms, early
+// publication, per-column warp match (shared-memory OR) + popc + one counter
+// atomic per digit group, staging at rank in shared memory
+// (radix_kernel.cuh:118-294, ranker.cuh:61-170, scatter.cuh:159-202 of the
+// reference).
 #pragma once
 
 #include "onesweep.cuh"
@@ -310,9 +328,10 @@ __host__ __device__ constexpr int floor_log2(int x) { return x <= 1 ? 0 : 1 + fl
 // nothing outside shared memory, when a sub-bucket holds more than
 // GBSORT_SPLIT_MAX keys (repeated keys, or keys that share those bits): the
 // per-digit bucket sort takes those.
-// One word per sub-bucket at ctr (2^RB <= CTR_WORDS words, left zeroed;
-// here the warp histograms and the match words after them): the count,
-// then start << 16 | cursor (cnt < 2^16).  Sub-bucket b lives in word
+// One word per sub-bucket at ctr (2^RB <= CTR_WORDS words, zero on entry
+// and left zeroed; here the warp histograms and the match words after
+// them, cleared before the grid barrier that precedes the buckets): the
+// count, then start << 16 | cursor (cnt < 2^16).  Sub-bucket b lives in word
 // b ^ ((b >> 5) & 31), which puts the scan's runs of 2^k consecutive
 // sub-buckets per thread on distinct banks.
 __host__ __device__ constexpr int split_slot(int b) { return b ^ ((b >> 5) & 31); }
@@ -336,9 +355,7 @@ __device__ __forceinline__ bool cta_bucket_split(const typename KeyBits<KB>::U (
     U* sk = reinterpret_cast<U*>(buf);
     auto slot = [](U k) { return split_slot(int(uint32_t(k >> SHIFT) & uint32_t(BINS - 1))); };
     auto valid = [&](int u) { return uint32_t(u * THREADS + tid) < cnt; };
-    for (int i = tid; i < BINS; i += THREADS) ctr[i] = 0u;
     if (tid == 0) *largest = 0u;
-    __syncthreads();
 #pragma unroll
     for (int u = 0; u < LIPT; ++u)
         if (valid(u)) atomicAdd(&ctr[slot(keys[u])], 1u);
@@ -592,16 +609,16 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) fused_short_kernel(FusedPar
             }
         }
         const uint32_t ex = block_exclusive_scan_256<uint32_t>(c, scan, nullptr);
-        if (tid < 256) {
-            binb[tid] = ex;
-            gbase[tid] = g;
-        }
+        if (tid < 256) binb[tid] = ex;
         __syncthreads();
 #pragma unroll
         for (int u = 0; u < IPT; ++u)
             if (uint32_t(u * THREADS + tid) < cnt) stage[binb[digit_of(keys[u], q)] + slot[u]] = keys[u];
+        if (tid < 256) gbase[tid] = g;  // the claim's answer: only the write-out needs it
         __syncthreads();
-        // coalesced runs, one per digit
+        // coalesced runs, one per digit (each key straight from registers
+        // to its region measured slower: 2^20 u32 26.1 vs 23.7 us, partial
+        // sector stores from every CTA at once)
         for (uint32_t j = tid; j < cnt; j += THREADS) {
             const U k = stage[j];
             const uint32_t d = digit_of(k, q);
@@ -619,7 +636,8 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) fused_short_kernel(FusedPar
     if (tid == 0) misc[0] = 0u;
     if constexpr (G::P >= 2) {
         if (f.msd) {
-            for (int i = tid; i < G::WARPS * 256; i += THREADS) mscratch[i] = 0u;  // the match words start zeroed
+            // the bucket sorts' counters and match words start zeroed
+            for (int i = tid; i < 2 * G::WARPS * 256; i += THREADS) whist[i] = 0u;
             U* regions = static_cast<U*>(f.regions);
             const uint32_t cap = f.region_cap;
             const U* src = static_cast<const U*>(p.copy_keys_in ? p.copy_keys_in : p.keys_a);
@@ -657,6 +675,8 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) fused_short_kernel(FusedPar
                         return;
                     cta_bucket_sort<KB, THREADS, LIPT>(regions + size_t(b) * cap, to, c, G::P - 1, smem, whist,
                                                        mscratch, scan, kind, desc);
+                    for (int i = tid; i < G::WARPS * 256; i += THREADS) whist[i] = 0u;  // the split's counters
+                    __syncthreads();
                 };
                 if (blockIdx.x < 256) sort_bucket(blockIdx.x, keys);
                 for (uint32_t b = blockIdx.x + gridDim.x; b < 256; b += gridDim.x) {

@@ -425,10 +425,8 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     // the one-launch short sort runs when its kernel can be made resident
     const bool fused =
         plan.fused.fn != nullptr && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0;
-    // it starts from cleared lookback status words too: they follow the
-    // control block, and both are cleared by one memset
-    const size_t clear_bytes = fused ? plan.status_off + plan.status_bytes - plan.ctl_off : plan.ctl.bytes;
-    cudaError_t e = cudaMemsetAsync(ctl, 0, clear_bytes, stream);
+    // (it clears its lookback status words itself, before its first pass)
+    cudaError_t e = cudaMemsetAsync(ctl, 0, plan.ctl.bytes, stream);
     if (e != cudaSuccess) return fail("memset control block", e);
 
     HistParams hp{};
@@ -986,6 +984,7 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
         out->pass_ctas = uint32_t(want < fmax ? want : fmax);
         out->hist_ctas = 0;  // counted by the same launch
         out->kernel_launches = 1;
+        out->msd_region_keys = g_short_msd.load(std::memory_order_relaxed) ? plan.msd_cap : 0u;
     }
     out->workspace_bytes = plan.total_bytes;
     return GBSORT_OK;

@@ -56,6 +56,7 @@ class PlanInfo(ctypes.Structure):
         ("threads", ctypes.c_uint32), ("items_per_thread", ctypes.c_uint32), ("num_tiles", ctypes.c_uint32),
         ("pass_ctas", ctypes.c_uint32), ("hist_ctas", ctypes.c_uint32), ("status_word_bytes", ctypes.c_uint32),
         ("kernel_launches", ctypes.c_uint32), ("workspace_bytes", ctypes.c_uint64),
+        ("msd_region_keys", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
     ]
 
 
@@ -234,6 +235,8 @@ class Plan:
     status_word_bytes: int
     kernel_launches: int
     workspace_bytes: int
+    msd_region_keys: int
+    reserved: int
 
 
 def plan(key_type, n: int, value_bytes: int = 0) -> Plan:

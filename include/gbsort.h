@@ -552,6 +552,11 @@ typedef struct gbsort_plan_info {
     uint32_t kernel_launches; /* launches (plus one memset node) per sort;
                                  1 when a short array sorts in one launch     */
     uint64_t workspace_bytes;
+    uint32_t msd_region_keys; /* one-launch sort, most significant digit
+                                 first: keys per top-digit region of its
+                                 partition (each key read and written twice);
+                                 0: every digit takes a pass                  */
+    uint32_t reserved;
 } gbsort_plan_info;
 
 int gbsort_plan(int key_type, size_t value_bytes, size_t n,

@@ -55,6 +55,16 @@ def test_plan_switch_and_oracle(gb, cuda, oracle, fused_default, n):
     assert _eq(gpu_sort(gb, cuda, "u32", raw), oracle.sort("u32", raw, False))
 
 
+def test_plan_reports_the_msd_regions(gb, fused_default, msd_default):
+    gb.set_short_msd(True)
+    info = gb.plan("u32", 1 << 20)
+    assert 4096 < info.msd_region_keys <= 8192  # the mean bucket plus a margin, within a CTA's local sort
+    assert gb.plan("u8", 1 << 20).msd_region_keys == 0  # one digit: nothing below it
+    assert gb.plan("u32", FUSED_MAX).msd_region_keys == 0  # buckets of ~8192 keys outgrow the local sort
+    gb.set_short_msd(False)
+    assert gb.plan("u32", 1 << 20).msd_region_keys == 0
+
+
 def test_values_and_long_arrays_keep_the_multi_launch_path(gb, fused_default):
     assert gb.plan("u32", 1 << 20, 4).kernel_launches > 1
     assert gb.plan("u64", FUSED_MAX + 1).kernel_launches > 1
