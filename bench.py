@@ -73,7 +73,8 @@ CONFIGS = {
     "c3a": dict(key="u64", n=1 << 27, dist=2, vb=8, desc=True,
                 workload="u64 keys (upper 32 bits from 256 values) + u64 index values, n=2^27, descending"),
     "c3b": dict(key="u128", n=1 << 26, dist=0, vb=0, desc=True,
-                workload="u128 keys (two uniform 64-bit halves), keys-only, n=2^26, descending"),
+                workload="u128 keys (two uniform 64-bit halves), keys-only, n=2^26, descending "
+                         "(most significant digit first: two splits + local sorts of 65536 groups)"),
     "c4": dict(key="u32", n=0, dist=0, vb=4, desc=False, segments=4096, seg_log2=(8, 20),
                workload="batched: 4096 independent u32-key/u32-value sorts, segment lengths log-uniform in "
                         "[2^8, 2^20] (seeded), keys uniform 32-bit, ascending, one batched run per step"),
@@ -448,8 +449,31 @@ def bench_gbsort(args, cfg, world, rank, local):
     sort_bytes = n * (kbytes + passes * 2 * (kbytes + vb))
     mean_sort_ms = total_ms / args.steps
     fused = all(len(p) == 1 for p in per_kernel)  # the whole short sort in one launch
-    msd_keys = gbsort.plan(kt, n, vb).msd_region_keys if fused else 0
-    if fused and msd_keys:
+    pinfo = gbsort.plan(kt, n, vb)
+    msd_keys = pinfo.msd_region_keys if fused else 0
+    stages = None
+    if not fused and pinfo.msd_stages:
+        # keys only, most significant digit first: the top digit's histogram
+        # (K bytes a key), top split (2K), pair count (K), scan, second split
+        # (2K), local sorts (2K); the other digits' histogram and the digit
+        # passes exit at once
+        names = ["msd_top_kernel (top split)", "msd_count_kernel (pair count)", "msd_scan_kernel (group offsets)",
+                 "msd_second_kernel (second split)", "msd_local_kernel (local sorts)"]
+        nbytes = [2 * kbytes * n, kbytes * n, 65536 * 8, 2 * kbytes * n, 2 * kbytes * n]
+        means = [statistics.mean(p[1 + i] for p in per_kernel) for i in range(5)]
+        dom = max(range(5), key=lambda i: means[i])
+        ups_ms = statistics.mean(p[0] for p in per_kernel)
+        launch_ms, launch_bytes, kernel = means[dom], nbytes[dom], names[dom]
+        sort_bytes = n * 8 * kbytes
+        stages = {"upsweep (top digit)": round(ups_ms, 4)}
+        for i in range(5):
+            stages[names[i]] = {"ms": round(means[i], 4),
+                                "frac": round(nbytes[i] / (means[i] / 1e3) / 1e9 / hbm, 4) if i != 2 else None}
+        rest = [statistics.mean(p[i] for p in per_kernel) for i in range(6, len(per_kernel[0]))]
+        stages["other digits' histogram + digit passes + fix-up (exit at once)"] = round(sum(rest), 4)
+    if stages is not None:
+        pass
+    elif fused and msd_keys:
         # most significant digit first: every key read, written to its
         # top-digit region, read back by its bucket's CTA, written home
         launch_ms = statistics.mean(p[0] for p in per_kernel)
@@ -469,6 +493,8 @@ def bench_gbsort(args, cfg, world, rank, local):
                 else "fallback 6.8 TB/s", "algorithmic_bytes_per_launch": launch_bytes,
                 "mean_launch_ms": round(launch_ms, 4), "upsweep_ms": None if ups_ms is None else round(ups_ms, 4),
                 "traffic_source": traffic_src}
+    if stages is not None:
+        roofline["msd_stages"] = stages
     sort_roofline = {"bytes_per_key": sort_bytes // n, "achieved": round(
         sort_bytes / (mean_sort_ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
         "frac": round(sort_bytes / (mean_sort_ms / 1e3) / 1e9 / hbm, 4)}
@@ -588,7 +614,8 @@ def bench_gbsort(args, cfg, world, rank, local):
         "gpu_launches": args.steps * (plan.kernel_launches + 1 + (1 if vb else 0)),
         "gpu_launches_note": "per step: generate (+values), then the sort's upsweep, one pass per key byte and "
                              "the pass-skip fix-up copy (exits at once when no pass was skipped), or for short "
-                             "keys-only arrays one launch doing all of it; plus one memset",
+                             "keys-only arrays one launch doing all of it, or for large keys-only 8- and 16-byte "
+                             "keys also the six MSD kernels (the passes then exit at once); plus one memset",
         "sorted_check": ok,
     }
     return line

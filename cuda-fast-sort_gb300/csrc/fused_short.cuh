@@ -336,13 +336,13 @@ __host__ __device__ constexpr int floor_log2(int x) { return x <= 1 ? 0 : 1 + fl
 // sub-buckets per thread on distinct banks.
 __host__ __device__ constexpr int split_slot(int b) { return b ^ ((b >> 5) & 31); }
 
-template <int KB, int THREADS, int LIPT, int CTR_WORDS>
+template <int KB, int THREADS, int LIPT, int CTR_WORDS, int BELOW = 8 * (KB - 1)>
 __device__ __forceinline__ bool cta_bucket_split(const typename KeyBits<KB>::U (&keys)[LIPT],
                                                  typename KeyBits<KB>::U* dst, uint32_t cnt, uint8_t* buf,
                                                  uint32_t* ctr, uint32_t* scan, uint32_t* largest, int kind,
                                                  int desc) {
     using U = typename KeyBits<KB>::U;
-    constexpr int BELOW = 8 * (KB - 1);  // key bits below the bucket's digit
+    // BELOW: key bits below the bits the bucket's keys share (its top digit)
     constexpr int RB_CAP = floor_log2(CTR_WORDS);
     constexpr int RB = RB_CAP < BELOW ? RB_CAP : BELOW;
     constexpr int BINS = 1 << RB;

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "fused_short.cuh"
+#include "msd.cuh"
 #include "onesweep.cuh"
 #include "segmented.cuh"
 #include "shapes.h"
@@ -53,6 +54,37 @@ const KernelEntry* fused_entry_for() {
         reinterpret_cast<const void*>(&fused_short_kernel<KB, S::THREADS, S::IPT, S::LIPT, S::MIN_CTAS>), S::THREADS,
         S::IPT, G::TILE, static_cast<unsigned long>(G::SMEM_BYTES)};
     return &e;
+}
+
+// Keys-only sorts of 8- and 16-byte keys, most significant digit first:
+// top split, pair count, scan, second split, local sorts (shape 0), local
+// sorts (shape 1).
+template <int KB, int L>
+KernelEntry make_msd_local_entry() {
+    using S = MsdShape<KB>;
+    using GL = MsdLocalGeom<KB, S::C_THREADS, S::C_LIPT[L]>;
+    return KernelEntry{reinterpret_cast<const void*>(&msd_local_kernel<KB, S::C_THREADS, S::C_LIPT[L],
+                                                                        S::C_MIN_CTAS[L], S::C_SPLIT_WORDS[L]>),
+                       S::C_THREADS, S::C_LIPT[L], S::C_THREADS * S::C_LIPT[L],
+                       static_cast<unsigned long>(GL::SMEM_BYTES)};
+}
+
+template <int KB>
+const KernelEntry* msd_entries_for() {
+    using S = MsdShape<KB>;
+    using GS = MsdSplitGeom<KB, S::THREADS, S::IPT>;
+    static const KernelEntry e[6] = {
+        {reinterpret_cast<const void*>(&msd_top_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
+         GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
+        {reinterpret_cast<const void*>(&msd_count_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
+         GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
+        {reinterpret_cast<const void*>(&msd_scan_kernel<KB>), MSD_SCAN_THREADS, 0, 0, 0ul},
+        {reinterpret_cast<const void*>(&msd_second_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
+         GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
+        make_msd_local_entry<KB, 0>(),
+        make_msd_local_entry<KB, 1>(),
+    };
+    return e;
 }
 
 template <int KB>

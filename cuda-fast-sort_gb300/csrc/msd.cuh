@@ -1,0 +1,371 @@
+// msd.cuh — keys-only sorts of 8- and 16-byte keys, most significant digit
+// first (sm_103a).
+//
+// A least-significant-digit sort of 16-byte keys makes 16 passes over the
+// data (8 for 8-byte keys), each bound by its stable rank.  Keys only, equal
+// twiddled keys are equal bytes, so the order among equal keys cannot show
+// and no step needs a stable order.  This path instead:
+//   top split:    every tile counts its keys per top digit with shared
+//                 atomics, claims its places in the digit's range (exact: the
+//                 upsweep's counts) with one global atomic per digit, stages
+//                 the tile by digit and writes each digit's run — no tile
+//                 waits for another (input -> alternate buffer, twiddled);
+//   pair count:   tiles of each top bucket count the second digit into
+//                 per-(top, second) totals;
+//   scan:         one CTA turns the 65536 totals into group offsets and
+//                 decides: every group fits a CTA's local sort (MSD_OK), or
+//                 not (MSD_OFF);
+//   second split: as the top split, within each top bucket, into the groups'
+//                 exact ranges (alternate buffer -> caller's buffer);
+//   local sorts:  each CTA sorts whole groups in place in shared memory (the
+//                 bucket split of fused_short.cuh: a counting pass on the next
+//                 12 bits, then a comparison rank inside the sub-buckets; or a
+//                 ranked pass per remaining digit where a sub-bucket is big)
+//                 and writes them untwiddled.
+// With MSD_OFF the least-significant-digit passes, launched after these
+// kernels, run from the untouched input; with MSD_OK they exit at once.
+// Every key is read and written three times (plus the upsweep's and the pair
+// count's reads): 16-byte keys 2^26 measured 0.38 ms per split against 0.54
+// ms per digit pass.
+#pragma once
+
+#include "fused_short.cuh"
+
+namespace gbsort {
+
+struct MsdParams {
+    const void* keys_in;   // the top split's input: the caller's keys or the input-preserving source
+    void* keys_a;          // the caller's buffer (second split's output, sorted in place)
+    void* keys_b;          // the alternate buffer (top split's output)
+    uint64_t n;
+    int kind, desc;
+    const unsigned long long* gp_top;  // the upsweep's counts of the top digit [256]
+    uint32_t* state;       // MSD_OK / MSD_OFF, zeroed before the sort
+    uint32_t* cursor1;     // [256] claimed places per top digit, zeroed
+    uint32_t* joint;       // [256 * 256] keys per (top, second) digit, zeroed
+    uint32_t* cursor2;     // [256 * 256] claimed places per group, zeroed
+    uint32_t* offs2;       // [256 * 256] first place of every group
+    uint32_t group_cap;    // largest group a local sort takes
+    uint32_t* err;         // workspace error word
+};
+
+// One tile split by one digit: `cnt` keys at src (twiddled on load when
+// TWIDDLE) go to dst at base[d] + (their place among the keys of digit d
+// that every tile claims from claim[d]), d = the key's digit `q`.  No order
+// among a digit's keys.  Shared: stage (the tile), bins / delta / scan.
+template <int KB, int THREADS, int IPT, bool TWIDDLE, class Base>
+__device__ __forceinline__ void msd_split_tile(const typename KeyBits<KB>::U* src, uint32_t cnt, int q, int kind,
+                                               int desc, uint32_t* claim, Base base, typename KeyBits<KB>::U* dst,
+                                               uint64_t n, uint32_t* err, typename KeyBits<KB>::U* stage,
+                                               uint32_t* bins, uint32_t* delta, uint32_t* scan) {
+    using U = typename KeyBits<KB>::U;
+    const int tid = threadIdx.x;
+    U keys[IPT];
+    uint32_t slot[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+        const uint32_t j = uint32_t(u * THREADS + tid);
+        keys[u] = U(0);
+        if (j < cnt) keys[u] = TWIDDLE ? twiddle_in<U>(src[j], kind, desc) : src[j];
+    }
+    if (tid < 256) bins[tid] = 0u;
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < IPT; ++u)
+        if (uint32_t(u * THREADS + tid) < cnt) slot[u] = atomicAdd(&bins[digit_of(keys[u], q)], 1u);
+    __syncthreads();
+    uint32_t c = 0, g = 0;
+    if (tid < 256) {
+        c = bins[tid];
+        if (c) g = atomicAdd(claim + tid, c);
+    }
+    const uint32_t ex = block_exclusive_scan_256<uint32_t>(c, scan, nullptr);
+    if (tid < 256) bins[tid] = ex;
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < IPT; ++u)
+        if (uint32_t(u * THREADS + tid) < cnt) stage[bins[digit_of(keys[u], q)] + slot[u]] = keys[u];
+    if (tid < 256) delta[tid] = base(tid) + g - ex;  // the claim's answer: only the write-out needs it
+    __syncthreads();
+    bool bad = false;
+    for (uint32_t j = tid; j < cnt; j += THREADS) {  // coalesced runs, one per digit
+        const U k = stage[j];
+        const uint32_t pos = delta[digit_of(k, q)] + j;
+        if (pos < n) dst[pos] = k;
+        else bad = true;
+    }
+    if (bad) atomicOr(err, ERRBIT_BOUNDS);
+    __syncthreads();  // the stage and the digit words are free for the next tile
+}
+
+// Every top bucket's first key, size and first tile of the second level
+// (tiles of `tile` keys that never cross a bucket), from the upsweep's
+// counts; tfirst[256] = the number of tiles.
+__device__ __forceinline__ void msd_top_table(const unsigned long long* gp_top, uint32_t tile, uint32_t* tstart,
+                                              uint32_t* tcnt, uint32_t* tfirst, uint32_t* scan) {
+    const int tid = threadIdx.x;
+    const uint32_t c = (tid < 256) ? uint32_t(gp_top[tid]) : 0u;
+    const uint32_t ex = block_exclusive_scan_256<uint32_t>(c, scan, nullptr);
+    __syncthreads();  // the scan words are read by every thread before the next scan writes them
+    uint32_t tiles = 0;
+    const uint32_t tex = block_exclusive_scan_256<uint32_t>((c + tile - 1) / tile, scan, &tiles);
+    if (tid < 256) {
+        tstart[tid] = ex;
+        tcnt[tid] = c;
+        tfirst[tid] = tex;
+    }
+    if (tid == 0) tfirst[256] = tiles;
+    __syncthreads();
+}
+
+// The top bucket of second-level tile t: the last b with tfirst[b] <= t.
+__device__ __forceinline__ uint32_t msd_bucket_of(const uint32_t* tfirst, uint32_t t) {
+    uint32_t lo = 0, hi = 256;  // tfirst[lo] <= t < tfirst[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (tfirst[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int KB, int THREADS, int IPT>
+struct MsdSplitGeom {
+    static constexpr int TILE = THREADS * IPT;
+    static constexpr size_t STAGE_BYTES = size_t(TILE) * KB;
+    static constexpr size_t WORDS_OFF = STAGE_BYTES;  // u32 bins[256], delta[256], tstart, tcnt, tfirst[257], scan[32]
+    static constexpr size_t SMEM_BYTES = WORDS_OFF + (256 * 5 + 1 + 32 + 4) * 4;
+};
+
+// Top split.  A top bucket holding more than 256 groups' worth of keys must
+// leave some group too big for a local sort: then MSD_OFF at once.
+template <int KB, int THREADS, int IPT, int MIN_CTAS>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_top_kernel(MsdParams p) {
+    using U = typename KeyBits<KB>::U;
+    using G = MsdSplitGeom<KB, THREADS, IPT>;
+    extern __shared__ __align__(128) uint8_t smem[];
+    U* stage = reinterpret_cast<U*>(smem);
+    uint32_t* bins = reinterpret_cast<uint32_t*>(smem + G::WORDS_OFF);
+    uint32_t* delta = bins + 256;
+    uint32_t* tstart = delta + 256;
+    uint32_t* scan = tstart + 256 * 3 + 1;
+    uint32_t* flag = scan + 32;
+    grid_launch_dependents();
+    grid_dependency_wait();
+    const int tid = threadIdx.x;
+    if (tid == 0) *flag = 0u;
+    const uint32_t c = (tid < 256) ? uint32_t(p.gp_top[tid]) : 0u;
+    const uint32_t ex = block_exclusive_scan_256<uint32_t>(c, scan, nullptr);
+    if (tid < 256) {
+        tstart[tid] = ex;
+        if (c > 256u * p.group_cap) atomicOr(flag, 1u);
+    }
+    __syncthreads();
+    if (*flag) {
+        if (blockIdx.x == 0 && tid == 0) *p.state = MSD_OFF;
+        return;
+    }
+    const U* in = static_cast<const U*>(p.keys_in);
+    U* out = static_cast<U*>(p.keys_b);
+    const uint64_t n = p.n;
+    const uint32_t T = uint32_t((n + G::TILE - 1) / G::TILE);
+    for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+        const uint64_t base = uint64_t(t) * G::TILE;
+        const uint32_t cnt = (n - base) < uint64_t(G::TILE) ? uint32_t(n - base) : uint32_t(G::TILE);
+        msd_split_tile<KB, THREADS, IPT, true>(in + base, cnt, KB - 1, p.kind, p.desc, p.cursor1,
+                                               [&](int d) { return tstart[d]; }, out, n, p.err, stage, bins, delta,
+                                               scan);
+    }
+}
+
+// Pair count: keys per (top, second) digit.
+template <int KB, int THREADS, int IPT, int MIN_CTAS>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_count_kernel(MsdParams p) {
+    using U = typename KeyBits<KB>::U;
+    using G = MsdSplitGeom<KB, THREADS, IPT>;
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint32_t* bins = reinterpret_cast<uint32_t*>(smem + G::WORDS_OFF);
+    uint32_t* tstart = bins + 512;
+    uint32_t* tcnt = tstart + 256;
+    uint32_t* tfirst = tcnt + 256;
+    uint32_t* scan = tfirst + 257;
+    grid_launch_dependents();
+    grid_dependency_wait();
+    if (ld_relaxed(p.state) == MSD_OFF) return;
+    const int tid = threadIdx.x;
+    msd_top_table(p.gp_top, G::TILE, tstart, tcnt, tfirst, scan);
+    const U* keys = static_cast<const U*>(p.keys_b);
+    const uint32_t T = tfirst[256];
+    for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+        const uint32_t b = msd_bucket_of(tfirst, t);
+        const uint32_t off = tstart[b] + (t - tfirst[b]) * G::TILE;
+        const uint32_t end = tstart[b] + tcnt[b];
+        const uint32_t cnt = (end - off) < uint32_t(G::TILE) ? end - off : uint32_t(G::TILE);
+        U k[IPT];
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            const uint32_t j = uint32_t(u * THREADS + tid);
+            k[u] = (j < cnt) ? keys[off + j] : U(0);
+        }
+        if (tid < 256) bins[tid] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < IPT; ++u)
+            if (uint32_t(u * THREADS + tid) < cnt) atomicAdd(&bins[digit_of(k[u], KB - 2)], 1u);
+        __syncthreads();
+        if (tid < 256 && bins[tid]) atomicAdd(p.joint + b * 256 + tid, bins[tid]);
+        __syncthreads();
+    }
+}
+
+// Scan of the 65536 group sizes (one CTA of 1024 threads, 64 groups each)
+// and the decision.
+constexpr int MSD_SCAN_THREADS = 1024;
+template <int KB>  // (one instance per key width's translation unit)
+__global__ void __launch_bounds__(MSD_SCAN_THREADS, 1) msd_scan_kernel(MsdParams p) {
+    __shared__ uint32_t scan[32];
+    __shared__ uint32_t biggest;
+    grid_launch_dependents();
+    grid_dependency_wait();
+    if (ld_relaxed(p.state) == MSD_OFF) return;
+    const int tid = threadIdx.x;
+    if (tid == 0) biggest = 0u;
+    constexpr int PER = 65536 / MSD_SCAN_THREADS;
+    const uint4* src = reinterpret_cast<const uint4*>(p.joint) + tid * (PER / 4);
+    uint32_t c[PER];
+#pragma unroll
+    for (int i = 0; i < PER / 4; ++i) {
+        const uint4 v = src[i];
+        c[4 * i] = v.x;
+        c[4 * i + 1] = v.y;
+        c[4 * i + 2] = v.z;
+        c[4 * i + 3] = v.w;
+    }
+    uint32_t sum = 0, big = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        sum += c[i];
+        big = max(big, c[i]);
+    }
+    uint32_t run = block_exclusive_scan_all<MSD_SCAN_THREADS>(sum, scan);
+    big = __reduce_max_sync(0xffffffffu, big);
+    if ((tid & 31) == 0) atomicMax(&biggest, big);
+    uint4* dst = reinterpret_cast<uint4*>(p.offs2) + tid * (PER / 4);
+#pragma unroll
+    for (int i = 0; i < PER / 4; ++i) {
+        uint4 v;
+        v.x = run;
+        run += c[4 * i];
+        v.y = run;
+        run += c[4 * i + 1];
+        v.z = run;
+        run += c[4 * i + 2];
+        v.w = run;
+        run += c[4 * i + 3];
+        dst[i] = v;
+    }
+    __syncthreads();
+    if (tid == 0) *p.state = (biggest <= p.group_cap) ? MSD_OK : MSD_OFF;
+}
+
+// Second split: within every top bucket, into the groups' ranges.
+template <int KB, int THREADS, int IPT, int MIN_CTAS>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_second_kernel(MsdParams p) {
+    using U = typename KeyBits<KB>::U;
+    using G = MsdSplitGeom<KB, THREADS, IPT>;
+    extern __shared__ __align__(128) uint8_t smem[];
+    U* stage = reinterpret_cast<U*>(smem);
+    uint32_t* bins = reinterpret_cast<uint32_t*>(smem + G::WORDS_OFF);
+    uint32_t* delta = bins + 256;
+    uint32_t* tstart = delta + 256;
+    uint32_t* tcnt = tstart + 256;
+    uint32_t* tfirst = tcnt + 256;
+    uint32_t* scan = tfirst + 257;
+    grid_launch_dependents();
+    grid_dependency_wait();
+    if (ld_relaxed(p.state) != MSD_OK) return;
+    msd_top_table(p.gp_top, G::TILE, tstart, tcnt, tfirst, scan);
+    const U* in = static_cast<const U*>(p.keys_b);
+    U* out = static_cast<U*>(p.keys_a);
+    const uint32_t T = tfirst[256];
+    for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+        const uint32_t b = msd_bucket_of(tfirst, t);
+        const uint32_t off = tstart[b] + (t - tfirst[b]) * G::TILE;
+        const uint32_t end = tstart[b] + tcnt[b];
+        const uint32_t cnt = (end - off) < uint32_t(G::TILE) ? end - off : uint32_t(G::TILE);
+        const uint32_t* group_base = p.offs2 + b * 256;
+        msd_split_tile<KB, THREADS, IPT, false>(in + off, cnt, KB - 2, p.kind, p.desc, p.cursor2 + b * 256,
+                                                [&](int d) { return group_base[d]; }, out, p.n, p.err, stage, bins,
+                                                delta, scan);
+    }
+}
+
+template <int KB, int THREADS, int LIPT>
+struct MsdLocalGeom {
+    static constexpr int WARPS = THREADS / 32;
+    static constexpr int CTR_WORDS = 2 * WARPS * 256;  // the split's sub-buckets, or warp histograms + match words
+    static constexpr size_t BUF_BYTES = (size_t(THREADS) * LIPT * KB + 127) & ~size_t(127);
+    static constexpr size_t CTR_OFF = BUF_BYTES;
+    static constexpr size_t SCAN_OFF = CTR_OFF + size_t(CTR_WORDS) * 4;  // u32 [32]
+    static constexpr size_t MISC_OFF = SCAN_OFF + 128;                    // u32 [4]
+    static constexpr size_t SMEM_BYTES = MISC_OFF + 16;
+};
+
+// Local sorts: each group (keys sharing their top two digits) sorted in
+// place; the split counts over SPLIT_WORDS sub-buckets (about twice the mean
+// group: fewer scan words per key, a comparison or two per key).
+template <int KB, int THREADS, int LIPT, int MIN_CTAS, int SPLIT_WORDS>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_local_kernel(MsdParams p) {
+    using U = typename KeyBits<KB>::U;
+    using G = MsdLocalGeom<KB, THREADS, LIPT>;
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint32_t* ctr = reinterpret_cast<uint32_t*>(smem + G::CTR_OFF);
+    uint32_t* scan = reinterpret_cast<uint32_t*>(smem + G::SCAN_OFF);
+    uint32_t* misc = reinterpret_cast<uint32_t*>(smem + G::MISC_OFF);
+    grid_launch_dependents();
+    grid_dependency_wait();
+    if (ld_relaxed(p.state) != MSD_OK) return;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < G::CTR_WORDS; i += THREADS) ctr[i] = 0u;
+    __syncthreads();
+    // Groups blockIdx.x, + gridDim.x, ...: the next group's size and place
+    // load one group ahead.  (Its keys too, into a second register set or
+    // into this one once the current keys sit in shared memory, measured
+    // slower: 16-byte keys 2^26 2.32 vs 2.15 ms, the extra live registers
+    // spill.)
+    U* keys = static_cast<U*>(p.keys_a);
+    U k[LIPT];
+    auto load = [&](uint32_t cnt, uint32_t off) {
+#pragma unroll
+        for (int u = 0; u < LIPT; ++u) {
+            const uint32_t j = uint32_t(u * THREADS + tid);
+            k[u] = (j < cnt) ? keys[off + j] : U(0);
+        }
+    };
+    uint32_t g = blockIdx.x;
+    uint32_t c = (g < 65536u) ? p.joint[g] : 0u, o = (g < 65536u) ? p.offs2[g] : 0u;
+    load(c, o);
+    while (g < 65536u) {
+        const uint32_t gn = g + gridDim.x;
+        const uint32_t cn = (gn < 65536u) ? p.joint[gn] : 0u, on = (gn < 65536u) ? p.offs2[gn] : 0u;
+        if (c != 0u) {
+            U* at = keys + o;
+            static_assert(SPLIT_WORDS <= G::CTR_WORDS, "the split's counters");
+            const bool split =
+                cta_bucket_split<KB, THREADS, LIPT, SPLIT_WORDS, 8 * (KB - 2)>(k, at, c, smem, ctr, scan, misc, p.kind,
+                                                                              p.desc);
+            if (!split) {
+                cta_bucket_sort<KB, THREADS, LIPT>(at, at, c, KB - 2, smem, ctr, ctr + G::WARPS * 256, scan, p.kind,
+                                                   p.desc);
+                for (int i = tid; i < G::WARPS * 256; i += THREADS) ctr[i] = 0u;  // the split's counters
+                __syncthreads();
+            }
+        }
+        load(cn, on);
+        g = gn;
+        c = cn;
+        o = on;
+    }
+}
+
+}  // namespace gbsort

@@ -69,6 +69,11 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
     for (int i = tid; i < G::NBINS * G::COPIES / 4; i += HIST_THREADS)
         reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
     grid_launch_dependents();  // the first pass may be scheduled; it waits for this grid
+    if (p.msd_state) {  // the digit passes' histogram after the MSD kernels
+        grid_dependency_wait();
+        if (ld_relaxed(p.msd_state) == MSD_OK) return;
+    }
+    const int dlo = p.digit_lo, dhi = p.digit_hi ? p.digit_hi : G::P;
 
     // Fused clears / copies that must precede the first pass.
     {
@@ -86,7 +91,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
         const U t = twiddle_in<U>(k, kind, desc);
 #pragma unroll
         for (int d = 0; d < G::P; ++d)
-            atomicAdd(&cnt[(d * 256 + digit_of(t, d)) * G::COPIES + copy], 1u);
+            if (d >= dlo && d < dhi) atomicAdd(&cnt[(d * 256 + digit_of(t, d)) * G::COPIES + copy], 1u);
     };
 
     const U* keys = static_cast<const U*>(p.keys);
@@ -125,7 +130,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
     __syncthreads();
 
     // Reduce the copies: one warp per bin, conflict-free row read.
-    for (int bin = warp; bin < G::NBINS; bin += HIST_THREADS / 32) {
+    for (int bin = dlo * 256 + warp; bin < dhi * 256; bin += HIST_THREADS / 32) {
         uint32_t s = (lane < G::COPIES) ? cnt[bin * G::COPIES + lane] : 0u;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -222,6 +227,7 @@ __device__ __forceinline__ void onesweep_pass_body(const PassParams& p, uint8_t*
     // successor never holds slots a CTA of this pass still needs.
     grid_launch_dependents();
     grid_dependency_wait();
+    if (p.msd_state && ld_relaxed(p.msd_state) == MSD_OK) return;  // the MSD kernels sorted
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // Tile position of item u of this thread: warp-striped (a warp's 32 lanes
@@ -724,6 +730,7 @@ __device__ __forceinline__ void grid_copy_bytes(void* dst, const void* src, uint
 // in the other buffer than the one it belongs in (in place: an odd count
 // left it in the alternate buffer); copy it across.  Otherwise nothing to do.
 __device__ __forceinline__ void fixup_body(const FixupParams& f) {
+    if (f.msd_state && ld_relaxed(f.msd_state) == MSD_OK) return;  // the MSD kernels sorted
     // the executed pass kernels left their count; none ran when the word is 0
     const uint32_t w = *f.executed;
     const int executed = (w >> 31) ? int(w & 0xFFu) : 0;

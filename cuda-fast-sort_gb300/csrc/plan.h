@@ -43,6 +43,18 @@ struct CtlLayout {
     }
 };
 
+// The MSD block of a keys-only sort of 8- or 16-byte keys (offsets from
+// Plan::msd_off; msd.cuh).
+struct MsdLayout {
+    static constexpr size_t STATE = 0;
+    static constexpr size_t CURSOR1 = 256;
+    static constexpr size_t JOINT = CURSOR1 + 256 * 4;
+    static constexpr size_t CURSOR2 = JOINT + 65536 * 4;
+    static constexpr size_t ZERO_BYTES = CURSOR2 + 65536 * 4;  // cleared by the upsweep
+    static constexpr size_t OFFS2 = ZERO_BYTES;
+    static constexpr size_t BYTES = OFFS2 + 65536 * 4;
+};
+
 struct Plan {
     int key_type = 0;
     int kb = 0;            // key bytes
@@ -66,6 +78,15 @@ struct Plan {
     // the one-launch sort's MSD regions: 256 x msd_cap keys (msd_cap 0: none)
     size_t regions_off = 0;
     uint32_t msd_cap = 0;
+    // keys-only sorts of 8- and 16-byte keys, most significant digit first
+    // (msd.cuh): kernels (top split, pair count, scan, second split, local
+    // sorts), group capacity, and the block at msd_off: state word (256 B),
+    // cursors [256], group sizes [65536], group cursors [65536] — zeroed by
+    // the upsweep — then group offsets [65536]
+    bool msd = false;
+    KernelEntry msd_k[5]{};
+    uint32_t msd_group_cap = 0;
+    size_t msd_off = 0;
     size_t total_bytes = 0;
     CtlLayout ctl{};
 };

@@ -89,6 +89,38 @@ constexpr int fused_local_tile(int kb) {
                       : FusedShape<16>::THREADS * FusedShape<16>::LIPT;
 }
 
+// Keys-only sorts of 8- and 16-byte keys, most significant digit first
+// (msd.cuh): the two splits' tiles (THREADS x IPT keys; 8-byte keys 2^27:
+// 2.95 ms with 24 keys per thread, 3.06 with 16, 3.03 with 32) and the local
+// sorts' CTAs (groups of up to C_THREADS x C_LIPT keys), for n in
+// [msd_n_min, msd_n_max] (groups of ~64 to ~2048 / ~384 to ~4096 keys;
+// outside, the digit passes).  Measured against the digit passes, CUDA
+// events, descending: 16-byte keys 2^22 0.58 vs 0.82 ms, 2^24 0.89 vs 2.46,
+// 2^26 2.11 vs 9.24; 8-byte keys 2^24 0.86 vs 0.82, 2^25 1.18 vs 1.52, 2^27
+// 2.95 vs 5.71.
+// Two local-sort shapes per width: L = 0 for groups of up to ~1024
+// (16-byte) / ~2048 (8-byte) keys on average, more CTAs per SM; L = 1 for
+// the larger groups up to msd_n_max.
+template <int KB>
+struct MsdShape {
+    static constexpr int THREADS = 256;
+    static constexpr int IPT = KB == 16 ? 12 : 24;
+    static constexpr int MIN_CTAS = 2;
+    static constexpr int C_THREADS = 256;
+    static constexpr int C_LIPT[2] = {KB == 16 ? 8 : 12, KB == 16 ? 12 : 24};
+    static constexpr int C_MIN_CTAS[2] = {3, 2};
+    static constexpr int C_SPLIT_WORDS[2] = {KB == 16 ? 2048 : 4096, 4096};
+};
+constexpr bool msd_key_bytes(int kb) { return kb == 8 || kb == 16; }
+constexpr uint64_t msd_n_min(int kb) { return kb == 16 ? uint64_t(1) << 22 : uint64_t(3) << 23; }
+constexpr uint64_t msd_n_max(int kb) { return kb == 16 ? uint64_t(1) << 27 : uint64_t(1) << 28; }
+// the local-sort shape for n keys (groups of n / 65536 on average)
+constexpr int msd_local_shape(int kb, uint64_t n) { return n <= (msd_n_max(kb) >> 1) ? 0 : 1; }
+constexpr uint32_t msd_group_cap(int kb, int shape) {
+    return kb == 16 ? uint32_t(MsdShape<16>::C_THREADS * MsdShape<16>::C_LIPT[shape])
+                    : uint32_t(MsdShape<8>::C_THREADS * MsdShape<8>::C_LIPT[shape]);
+}
+
 // Keys per MSD region of the one-launch sort (one region per top digit):
 // the mean bucket n/256 plus four of its standard deviations plus 64,
 // rounded up to 32 (uniform top digits overflow a region about once in

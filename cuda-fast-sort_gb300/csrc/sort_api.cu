@@ -25,6 +25,7 @@
 #include "plan.h"
 #include "device_common.cuh"
 #include "fused_short.cuh"
+#include "msd.cuh"
 #include "onesweep.cuh"
 #include "sort_params.h"
 
@@ -45,6 +46,18 @@ const KernelEntry* fused_entry_k2();
 const KernelEntry* fused_entry_k4();
 const KernelEntry* fused_entry_k8();
 const KernelEntry* fused_entry_k16();
+
+const KernelEntry* msd_entries_k8();
+const KernelEntry* msd_entries_k16();
+
+// Kernels of the MSD path of keys-only sorts (8- and 16-byte keys; msd.cuh).
+const KernelEntry* msd_entries(int kb) {
+    switch (kb) {
+        case 8: return msd_entries_k8();
+        case 16: return msd_entries_k16();
+        default: return nullptr;
+    }
+}
 
 const KernelEntry* fused_entry(int kb) {
     switch (kb) {
@@ -93,6 +106,13 @@ std::atomic<int> g_short_fused{[] {
 // switched off (gbsort_set_short_msd).
 std::atomic<int> g_short_msd{[] {
     const char* v = std::getenv("GBSORT_SHORT_MSD");
+    return (v && v[0] == '0') ? 0 : 1;
+}()};
+// Keys-only sorts of 8- and 16-byte keys above the short range, most
+// significant digit first (msd.cuh): on unless GBSORT_MSD=0 or switched off
+// (gbsort_set_msd).
+std::atomic<int> g_msd{[] {
+    const char* v = std::getenv("GBSORT_MSD");
     return (v && v[0] == '0') ? 0 : 1;
 }()};
 // Uniform-digit pass skipping: on unless GBSORT_PASS_SKIP=0 or switched off.
@@ -309,6 +329,21 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
             off = align_up(off + size_t(256) * p.msd_cap * kb, 256);
         }
     }
+    // keys-only sorts of 8- and 16-byte keys above the short range: the MSD
+    // block (sized whether or not the path is switched on), right after the
+    // status words so that the upsweep clears both in one sweep
+    if (!small && p.vb == 0 && msd_key_bytes(p.kb) && n >= msd_n_min(p.kb) && n <= msd_n_max(p.kb) &&
+        msd_entries(p.kb) != nullptr) {
+        p.msd_off = off;
+        off = align_up(off + MsdLayout::BYTES, 256);
+        const int shape = msd_local_shape(p.kb, n);
+        p.msd_group_cap = msd_group_cap(p.kb, shape);
+        if (g_msd.load(std::memory_order_relaxed)) {
+            p.msd = true;
+            for (int i = 0; i < 4; ++i) p.msd_k[i] = msd_entries(p.kb)[i];
+            p.msd_k[4] = msd_entries(p.kb)[4 + shape];
+        }
+    }
     p.total_bytes = off;
     *plan = p;
     return GBSORT_OK;
@@ -330,6 +365,10 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     if (st != GBSORT_OK) return st;
     st = prepare_kernel(plan.upsweep);
     if (st != GBSORT_OK) return st;
+    // the MSD path of keys-only sorts runs when all its kernels can
+    bool use_msd = plan.msd;
+    for (int i = 0; use_msd && i < 5; ++i) use_msd = prepare_kernel(plan.msd_k[i]) == GBSORT_OK;
+    const int ms_stages = use_msd ? 6 : 0;  // its five kernels and the other digits' histogram
 
     uint8_t* ws = static_cast<uint8_t*>(d_workspace);
     // a DoubleBuffer workspace starts at the control block
@@ -353,8 +392,8 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     // a DoubleBuffer sort when the executed passes' parity differs from the
     // pass count's
     const bool fixup = skip && (alt != nullptr || (plan.passes & 1) == 0 || copy);
-    const int nev = plan.passes + 2 + (fixup ? 1 : 0);
-    cudaEvent_t ev[20] = {};
+    const int nev = plan.passes + 2 + ms_stages + (fixup ? 1 : 0);
+    cudaEvent_t ev[32] = {};
     const bool timed = ms != nullptr;
     if (timed) {
         for (int i = 0; i < nev; ++i) {
@@ -367,6 +406,10 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
             for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
         return GBSORT_ERR_CUDA;
     };
+
+    // the MSD block (keys-only sorts of 8- and 16-byte keys)
+    uint8_t* msd_block = use_msd ? ws + plan.msd_off - ws_base : nullptr;
+    const uint32_t* msd_state = use_msd ? reinterpret_cast<const uint32_t*>(msd_block + MsdLayout::STATE) : nullptr;
 
     // Parameters of digit pass `pass` and of the fix-up copy.
     auto pass_params = [&](int pass) {
@@ -404,6 +447,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         pp.copy_keys_in = copy ? keys_src : nullptr;
         pp.copy_vals_in = copy ? vals_src : nullptr;
         pp.executed = fixup ? reinterpret_cast<uint32_t*>(ctl + plan.ctl.exec_off) : nullptr;
+        pp.msd_state = msd_state;
         return pp;
     };
     auto fixup_params = [&] {
@@ -419,6 +463,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         fp.copy_keys_in = copy ? keys_src : nullptr;
         fp.copy_vals_in = copy ? vals_src : nullptr;
         fp.want_odd = alt ? (plan.passes & 1) : 0;
+        fp.msd_state = msd_state;
         return fp;
     };
 
@@ -436,11 +481,16 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     hp.desc = descending;
     hp.gp_counts = gp;
     hp.status = status;
-    hp.status_bytes = plan.status_bytes;
+    // the MSD block's counters follow the status words: one clear for both
+    hp.status_bytes = use_msd ? plan.msd_off + MsdLayout::ZERO_BYTES - plan.status_off : plan.status_bytes;
     hp.mirror_keys = odd ? alt_keys : nullptr;
     hp.vals = copy ? vals_src : d_values;
     hp.mirror_vals = (odd && plan.vb) ? alt_vals : nullptr;
     hp.val_bytes_total = plan.n * uint64_t(plan.vb);
+    if (use_msd) {  // the MSD path needs the top digit's counts only; the rest follow if it falls back
+        hp.digit_lo = plan.passes - 1;
+        hp.digit_hi = plan.passes;
+    }
     if (fused) {
         // Short array: the whole sort in one cooperative launch (every CTA
         // resident, or the launch fails; fused_short.cuh).
@@ -493,6 +543,45 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         if (e != cudaSuccess) return fail("upsweep launch", e);
         if (timed) cudaEventRecord(ev[1], stream);
     }
+    if (use_msd) {
+        // Keys only, 8- or 16-byte keys: top split, pair count, scan, second
+        // split, local sorts (msd.cuh); the digit passes below exit at once
+        // when these sorted, and sort from the untouched input otherwise.
+        MsdParams mp{};
+        mp.keys_in = copy ? keys_src : d_keys;
+        mp.keys_a = d_keys;
+        mp.keys_b = alt_keys;
+        mp.n = plan.n;
+        mp.kind = plan.kind;
+        mp.desc = descending;
+        mp.gp_top = gp + size_t(plan.passes - 1) * 256;
+        mp.state = reinterpret_cast<uint32_t*>(msd_block + MsdLayout::STATE);
+        mp.cursor1 = reinterpret_cast<uint32_t*>(msd_block + MsdLayout::CURSOR1);
+        mp.joint = reinterpret_cast<uint32_t*>(msd_block + MsdLayout::JOINT);
+        mp.cursor2 = reinterpret_cast<uint32_t*>(msd_block + MsdLayout::CURSOR2);
+        mp.offs2 = reinterpret_cast<uint32_t*>(msd_block + MsdLayout::OFFS2);
+        mp.group_cap = plan.msd_group_cap;
+        mp.err = err_word;
+        for (int i = 0; i < 5; ++i) {
+            const KernelEntry& k = plan.msd_k[i];
+            const uint64_t full = uint64_t(sms > 0 ? sms : 1) * uint64_t(resident_ctas(k) > 0 ? resident_ctas(k) : 1);
+            const uint32_t grid = (i == 2) ? 1u : uint32_t(full);
+            void* args[] = {&mp};
+            e = launch_dependent(k.fn, grid, k.threads, k.smem, stream, args);
+            if (e != cudaSuccess) return fail("msd launch", e);
+            if (timed) cudaEventRecord(ev[2 + i], stream);
+        }
+        // the other digits' counts, for the digit passes if they sort
+        HistParams rest = hp;
+        rest.digit_lo = 0;
+        rest.digit_hi = plan.passes - 1;
+        rest.status_bytes = 0;  // cleared by the first histogram kernel
+        rest.msd_state = msd_state;
+        void* args[] = {&rest};
+        e = launch_dependent(plan.upsweep.fn, hist_ctas, plan.upsweep.threads, plan.upsweep.smem, stream, args);
+        if (e != cudaSuccess) return fail("histogram launch", e);
+        if (timed) cudaEventRecord(ev[2 + 5], stream);
+    }
 
     const int occ = resident_ctas(plan.pass);
     const uint64_t max_ctas = uint64_t(sms) * uint64_t(occ > 0 ? occ : 1);
@@ -502,7 +591,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         void* args[] = {&pp};
         e = launch_dependent(plan.pass.fn, pass_ctas, plan.pass.threads, plan.pass.smem, stream, args);
         if (e != cudaSuccess) return fail("pass launch", e);
-        if (timed) cudaEventRecord(ev[2 + pass], stream);
+        if (timed) cudaEventRecord(ev[2 + ms_stages + pass], stream);
     }
     if (fixup) {
         FixupParams fp = fixup_params();
@@ -510,7 +599,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
         e = launch_dependent(reinterpret_cast<const void*>(&skip_fixup_kernel), uint32_t(sms > 0 ? sms : 1), 256, 0,
                              stream, args);
         if (e != cudaSuccess) return fail("fixup launch", e);
-        if (timed) cudaEventRecord(ev[2 + plan.passes], stream);
+        if (timed) cudaEventRecord(ev[2 + ms_stages + plan.passes], stream);
     }
 
     if (timed) {
@@ -565,14 +654,14 @@ int check_args(int key_type, size_t value_bytes, void* d_keys, void* d_values, s
 // graph, if any, is destroyed; one still running is freed by CUDA when it
 // completes).  gbsort_graph_cache_clear() frees them all.
 struct GraphKey {
-    int device, key_type, desc, skip, fused, msd;
+    int device, key_type, desc, skip, fused, msd, large_msd;
     size_t vb;
     uint64_t n, wait_limit;
     const void *keys, *vals, *ws, *ksrc, *vsrc, *keys_b, *vals_b;
     cudaStream_t stream;
     auto tie() const {
-        return std::tie(device, key_type, desc, skip, fused, msd, vb, n, wait_limit, keys, vals, ws, ksrc, vsrc,
-                        keys_b, vals_b, stream);
+        return std::tie(device, key_type, desc, skip, fused, msd, large_msd, vb, n, wait_limit, keys, vals, ws, ksrc,
+                        vsrc, keys_b, vals_b, stream);
     }
     bool operator==(const GraphKey& o) const { return tie() == o.tie(); }
 };
@@ -611,6 +700,7 @@ int launch_sort(const Plan& plan, int descending, void* keys, void* vals, void* 
     k.skip = g_pass_skip.load(std::memory_order_relaxed);
     k.fused = plan.fused.fn != nullptr;
     k.msd = g_short_msd.load(std::memory_order_relaxed);
+    k.large_msd = plan.msd ? 1 : 0;
     k.vb = size_t(plan.vb);
     k.n = plan.n;
     k.wait_limit = wait_limit_ns();
@@ -949,6 +1039,8 @@ void gbsort_graph_cache_stats(uint64_t* calls, uint64_t* graphs, uint64_t* captu
 
 void gbsort_set_pass_skip(int enable) { g_pass_skip.store(enable ? 1 : 0, std::memory_order_relaxed); }
 int gbsort_get_pass_skip(void) { return g_pass_skip.load(std::memory_order_relaxed); }
+void gbsort_set_msd(int enable) { g_msd.store(enable ? 1 : 0, std::memory_order_relaxed); }
+int gbsort_get_msd(void) { return g_msd.load(std::memory_order_relaxed); }
 void gbsort_set_short_fused(int enable) { g_short_fused.store(enable ? 1 : 0, std::memory_order_relaxed); }
 int gbsort_get_short_fused(void) { return g_short_fused.load(std::memory_order_relaxed); }
 void gbsort_set_short_msd(int enable) { g_short_msd.store(enable ? 1 : 0, std::memory_order_relaxed); }
@@ -977,6 +1069,10 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n, gbsort_plan_info* ou
     }
     out->status_word_bytes = plan.wide_status ? 8 : 4;
     out->kernel_launches = uint32_t(plan.passes + 1 + ((gbsort_get_pass_skip() && (plan.passes & 1) == 0) ? 1 : 0));
+    if (plan.msd) {
+        out->msd_stages = 6;
+        out->kernel_launches += 6;
+    }
     if (plan.fused.fn && sms > 0 && prepare_kernel(plan.fused) == GBSORT_OK && resident_ctas(plan.fused) > 0) {
         const uint64_t fmax = uint64_t(sms) * uint64_t(resident_ctas(plan.fused));
         uint64_t want = plan.num_tiles;

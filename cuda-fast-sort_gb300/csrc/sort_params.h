@@ -5,6 +5,11 @@
 
 namespace gbsort {
 
+// Outcome of the most-significant-digit-first path of a keys-only sort
+// (msd.cuh): 0 undecided, MSD_OK the MSD kernels sort, MSD_OFF the digit
+// passes sort.
+constexpr uint32_t MSD_OK = 1u, MSD_OFF = 2u;
+
 // Global-histogram upsweep (one launch per sort).
 struct HistParams {
     const void* keys;           // user keys (raw bits)
@@ -20,6 +25,12 @@ struct HistParams {
     const void* vals;
     void* mirror_vals;
     uint64_t val_bytes_total;   // n * value bytes
+    // digits counted: [digit_lo, digit_hi), every digit when digit_hi == 0
+    int digit_lo, digit_hi;
+    // non-null: a histogram of the remaining digits for the digit passes of
+    // a keys-only sort whose MSD path may already have sorted: exits when it
+    // did (MSD_OK), waits for its predecessor kernel first
+    const uint32_t* msd_state;
 };
 
 // Batched mode: one entry per global tile, built on the host.
@@ -73,6 +84,8 @@ struct PassParams {
     const uint32_t* nonuniform_mask;
     // plain mode with skipping: receives bit 31 | number of executed passes
     uint32_t* executed;
+    // keys-only sorts with the MSD path: the pass exits when it sorted (MSD_OK)
+    const uint32_t* msd_state;
 };
 
 // The copy home after uniform-pass skipping left an odd number of executed
@@ -93,6 +106,8 @@ struct FixupParams {
     // input-preserving sort: when no pass ran, copy these to the output
     const void* copy_keys_in;
     const void* copy_vals_in;
+    // keys-only sorts with the MSD path: nothing to do when it sorted
+    const uint32_t* msd_state;
 };
 
 // One-launch sort of a short array (cooperative launch, every CTA resident):

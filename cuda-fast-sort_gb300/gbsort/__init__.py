@@ -56,7 +56,7 @@ class PlanInfo(ctypes.Structure):
         ("threads", ctypes.c_uint32), ("items_per_thread", ctypes.c_uint32), ("num_tiles", ctypes.c_uint32),
         ("pass_ctas", ctypes.c_uint32), ("hist_ctas", ctypes.c_uint32), ("status_word_bytes", ctypes.c_uint32),
         ("kernel_launches", ctypes.c_uint32), ("workspace_bytes", ctypes.c_uint64),
-        ("msd_region_keys", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+        ("msd_region_keys", ctypes.c_uint32), ("msd_stages", ctypes.c_uint32),
     ]
 
 
@@ -236,7 +236,7 @@ class Plan:
     kernel_launches: int
     workspace_bytes: int
     msd_region_keys: int
-    reserved: int
+    msd_stages: int
 
 
 def plan(key_type, n: int, value_bytes: int = 0) -> Plan:
@@ -609,6 +609,21 @@ def set_short_msd(enable: bool) -> None:
 
 def get_short_msd() -> bool:
     f = lib().gbsort_get_short_msd
+    f.restype = ctypes.c_int
+    return bool(f())
+
+
+def set_msd(enable: bool) -> None:
+    """Most-significant-digit-first path of large keys-only sorts of 8- and
+    16-byte keys on (default) or off."""
+    f = lib().gbsort_set_msd
+    f.restype = None
+    f.argtypes = [ctypes.c_int]
+    f(int(enable))
+
+
+def get_msd() -> bool:
+    f = lib().gbsort_get_msd
     f.restype = ctypes.c_int
     return bool(f())
 

@@ -466,15 +466,28 @@ int gbsort_get_pass_skip(void);
 void gbsort_set_short_fused(int enable);
 int gbsort_get_short_fused(void);
 
-/* Inside the one-launch short sort (keys of 2 bytes or more): when every
- * bucket of the most significant digit fits one CTA (8192 keys of 2 or 4
- * bytes, 5120 of 8, 2048 of 16), one pass partitions the keys by that digit
- * and each CTA then sorts whole buckets in shared memory over the remaining
- * digits — one grid-wide exchange instead of one per digit.  Otherwise (or
- * when switched off: GBSORT_SHORT_MSD=0, gbsort_set_short_msd(0)) every
- * digit takes a pass.  The stable sort's result either way. */
+/* Inside the one-launch short sort (keys of 2 bytes or more): when the
+ * top-digit regions fit a CTA's local sort (gbsort_plan_info.msd_region_keys
+ * != 0), every tile partitions its keys into them by the most significant
+ * digit and each CTA then sorts whole buckets in shared memory — one
+ * grid-wide exchange instead of one per digit.  Otherwise (or when switched
+ * off: GBSORT_SHORT_MSD=0, gbsort_set_short_msd(0)) every digit takes a
+ * pass.  Keys only, so the result is the same bytes either way. */
 void gbsort_set_short_msd(int enable);
 int gbsort_get_short_msd(void);
+
+/* Keys-only sorts of 8- and 16-byte keys above the short range (1.5 x 2^24
+ * to 2^28 keys of 8 bytes, 2^22 to 2^27 of 16): most significant digit first —
+ * a split by the top digit, a count of (top, second) digit pairs, a split by
+ * the second digit into the 65536 pairs' ranges, and in-place local sorts
+ * of those groups in shared memory — instead of one stable pass per key
+ * byte (gbsort_plan_info.msd_stages = 6).  When a group outgrows a local
+ * sort (skewed or repeated keys), the digit passes sort instead, decided on
+ * the device.  The size query reserves the path's ~1 MB either way.  On by
+ * default; GBSORT_MSD=0 in the environment or gbsort_set_msd(0) turns it
+ * off.  Keys only, so the result is the same bytes either way. */
+void gbsort_set_msd(int enable);
+int gbsort_get_msd(void);
 
 /* Graph replay of repeated calls (default on; GBSORT_GRAPH_CACHE=0 turns it
  * off at load).  The second call of gbsort_sort_keys / _pairs / _copy with
@@ -556,7 +569,15 @@ typedef struct gbsort_plan_info {
                                  first: keys per top-digit region of its
                                  partition (each key read and written twice);
                                  0: every digit takes a pass                  */
-    uint32_t reserved;
+    uint32_t msd_stages;      /* keys-only sorts of 8- and 16-byte keys above
+                                 the short range, most significant digit
+                                 first: 6 kernels (top split, pair count,
+                                 scan, second split, local sorts, and the
+                                 histogram of the other digits) run after the
+                                 top digit's histogram kernel and before the
+                                 digit passes; those and the last histogram
+                                 exit at once unless a group was too big;
+                                 0: not planned                              */
 } gbsort_plan_info;
 
 int gbsort_plan(int key_type, size_t value_bytes, size_t n,
@@ -565,11 +586,15 @@ int gbsort_plan(int key_type, size_t value_bytes, size_t n,
 /* Same as gbsort_sort_pairs (d_values may be NULL with value_bytes 0), but
  * records a CUDA event around every kernel on `stream` and, after
  * synchronizing, writes the per-kernel device milliseconds to ms_out:
- * ms_out[0] = histogram kernel, ms_out[1 + p] = digit pass p, and with pass
- * skipping on and an even pass count P, ms_out[1 + P] = the fix-up copy.  A
- * short array sorted in one launch (gbsort_set_short_fused) writes one entry,
- * the whole sort.  ms_cap is the
- * capacity of ms_out; *n_ms receives the number of entries written. */
+ * ms_out[0] = histogram kernel, then with the MSD path planned
+ * (gbsort_plan_info.msd_stages = S = 6) ms_out[1 .. S] = its kernels (top
+ * split, pair count, scan, second split, local sorts, histogram of the other
+ * digits), then
+ * ms_out[1 + S + p] = digit pass p (S = 0 otherwise), and with pass skipping
+ * on and an even pass count P, ms_out[1 + S + P] = the fix-up copy.  A short
+ * array sorted in one launch (gbsort_set_short_fused) writes one entry, the
+ * whole sort.  ms_cap is the capacity of ms_out; *n_ms receives the number
+ * of entries written. */
 int gbsort_sort_timed(int key_type, int descending, void* d_keys,
                       void* d_values, size_t value_bytes, void* d_workspace,
                       size_t temp_bytes, size_t n, void* stream,
