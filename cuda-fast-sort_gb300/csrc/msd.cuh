@@ -53,21 +53,27 @@ struct MsdParams {
 // TWIDDLE) go to dst at base[d] + (their place among the keys of digit d
 // that every tile claims from claim[d]), d = the key's digit `q`.  No order
 // among a digit's keys.  Shared: stage (the tile), bins / delta / scan.
-template <int KB, int THREADS, int IPT, bool TWIDDLE, class Base>
-__device__ __forceinline__ void msd_split_tile(const typename KeyBits<KB>::U* src, uint32_t cnt, int q, int kind,
-                                               int desc, uint32_t* claim, Base base, typename KeyBits<KB>::U* dst,
-                                               uint64_t n, uint32_t* err, typename KeyBits<KB>::U* stage,
-                                               uint32_t* bins, uint32_t* delta, uint32_t* scan) {
+template <int KB, int THREADS, int IPT, bool TWIDDLE>
+__device__ __forceinline__ void msd_load_tile(const typename KeyBits<KB>::U* src, uint32_t cnt, int kind, int desc,
+                                              typename KeyBits<KB>::U (&keys)[IPT]) {
     using U = typename KeyBits<KB>::U;
-    const int tid = threadIdx.x;
-    U keys[IPT];
-    uint32_t slot[IPT];
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
-        const uint32_t j = uint32_t(u * THREADS + tid);
+        const uint32_t j = uint32_t(u * THREADS + threadIdx.x);
         keys[u] = U(0);
         if (j < cnt) keys[u] = TWIDDLE ? twiddle_in<U>(src[j], kind, desc) : src[j];
     }
+}
+
+// The split of a tile whose keys are in registers (msd_load_tile's layout).
+template <int KB, int THREADS, int IPT, class Base>
+__device__ __forceinline__ void msd_split_loaded(const typename KeyBits<KB>::U (&keys)[IPT], uint32_t cnt, int q,
+                                                 uint32_t* claim, Base base, typename KeyBits<KB>::U* dst, uint64_t n,
+                                                 uint32_t* err, typename KeyBits<KB>::U* stage, uint32_t* bins,
+                                                 uint32_t* delta, uint32_t* scan) {
+    using U = typename KeyBits<KB>::U;
+    const int tid = threadIdx.x;
+    uint32_t slot[IPT];
     if (tid < 256) bins[tid] = 0u;
     __syncthreads();
 #pragma unroll
@@ -98,16 +104,14 @@ __device__ __forceinline__ void msd_split_tile(const typename KeyBits<KB>::U* sr
     __syncthreads();  // the stage and the digit words are free for the next tile
 }
 
-// Starts pulling `bytes` at p into L2: the top split of 8-byte keys does it
-// for its CTA's next tile while it works on this one (2^27 keys: 0.95 ->
-// 0.76 ms; ncu had it waiting on global loads, long-scoreboard stalls 10 per
-// issue against 3 in the second split).  16-byte keys' splits and the
-// second split measured slower with it (2^26 u128 top split 0.36 -> 0.47).
-__device__ __forceinline__ void prefetch_l2(const void* p, uint64_t bytes) {
-    const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(127);
-    const uintptr_t end = reinterpret_cast<uintptr_t>(p) + bytes;
-    for (uintptr_t q = a + uintptr_t(threadIdx.x) * 128; q < end; q += uintptr_t(blockDim.x) * 128)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+template <int KB, int THREADS, int IPT, bool TWIDDLE, class Base>
+__device__ __forceinline__ void msd_split_tile(const typename KeyBits<KB>::U* src, uint32_t cnt, int q, int kind,
+                                               int desc, uint32_t* claim, Base base, typename KeyBits<KB>::U* dst,
+                                               uint64_t n, uint32_t* err, typename KeyBits<KB>::U* stage,
+                                               uint32_t* bins, uint32_t* delta, uint32_t* scan) {
+    typename KeyBits<KB>::U keys[IPT];
+    msd_load_tile<KB, THREADS, IPT, TWIDDLE>(src, cnt, kind, desc, keys);
+    msd_split_loaded<KB, THREADS, IPT>(keys, cnt, q, claim, base, dst, n, err, stage, bins, delta, scan);
 }
 
 // Every top bucket's first key, size and first tile of the second level
@@ -181,16 +185,34 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_top_kernel(MsdParams p)
     U* out = static_cast<U*>(p.keys_b);
     const uint64_t n = p.n;
     const uint32_t T = uint32_t((n + G::TILE - 1) / G::TILE);
-    for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+    auto tile_cnt = [&](uint32_t t) {
         const uint64_t base = uint64_t(t) * G::TILE;
-        const uint32_t cnt = (n - base) < uint64_t(G::TILE) ? uint32_t(n - base) : uint32_t(G::TILE);
-        if (KB == 8 && t + gridDim.x < T) {
-            const uint64_t nb = uint64_t(t + gridDim.x) * G::TILE;
-            prefetch_l2(in + nb, ((n - nb) < uint64_t(G::TILE) ? n - nb : uint64_t(G::TILE)) * KB);
+        return (t >= T) ? 0u : (n - base) < uint64_t(G::TILE) ? uint32_t(n - base) : uint32_t(G::TILE);
+    };
+    auto base = [&](int d) { return tstart[d]; };
+    if constexpr (KB == 8) {
+        // 8-byte keys: the CTA's next tile loads into a second register set
+        // while it splits this one (2^27 keys: 0.95 -> 0.68 ms; ncu had the
+        // split waiting on global loads, 10 long-scoreboard stalls per issue
+        // against 3 in the second split).  16-byte keys measured slower so
+        // (2^26: 0.36 -> 0.56 ms).
+        U keys[IPT];
+        uint32_t t = blockIdx.x;
+        msd_load_tile<KB, THREADS, IPT, true>(in + uint64_t(t) * G::TILE, tile_cnt(t), p.kind, p.desc, keys);
+        for (; t < T; t += gridDim.x) {
+            U next[IPT];
+            const uint32_t tn = t + gridDim.x;
+            msd_load_tile<KB, THREADS, IPT, true>(in + uint64_t(tn < T ? tn : t) * G::TILE, tile_cnt(tn), p.kind,
+                                                  p.desc, next);
+            msd_split_loaded<KB, THREADS, IPT>(keys, tile_cnt(t), KB - 1, p.cursor1, base, out, n, p.err, stage,
+                                               bins, delta, scan);
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) keys[u] = next[u];
         }
-        msd_split_tile<KB, THREADS, IPT, true>(in + base, cnt, KB - 1, p.kind, p.desc, p.cursor1,
-                                               [&](int d) { return tstart[d]; }, out, n, p.err, stage, bins, delta,
-                                               scan);
+    } else {
+        for (uint32_t t = blockIdx.x; t < T; t += gridDim.x)
+            msd_split_tile<KB, THREADS, IPT, true>(in + uint64_t(t) * G::TILE, tile_cnt(t), KB - 1, p.kind, p.desc,
+                                                   p.cursor1, base, out, n, p.err, stage, bins, delta, scan);
     }
 }
 
@@ -327,6 +349,12 @@ struct MsdLocalGeom {
     static constexpr size_t SMEM_BYTES = MISC_OFF + 16;
 };
 
+// 1: each CTA pulls its next group into L2 while it sorts the current one
+// (2^26 u128 local sorts 0.795 -> 0.779 ms, 2^27 u64 1.048 -> 1.040).
+#ifndef GBSORT_MSD_LOCAL_L2
+#define GBSORT_MSD_LOCAL_L2 1
+#endif
+
 // Local sorts: each group (keys sharing their top two digits) sorted in
 // place; the split counts over SPLIT_WORDS sub-buckets (about twice the mean
 // group: fewer scan words per key, a comparison or two per key).
@@ -364,6 +392,14 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_local_kernel(MsdParams 
     while (g < 65536u) {
         const uint32_t gn = g + gridDim.x;
         const uint32_t cn = (gn < 65536u) ? p.joint[gn] : 0u, on = (gn < 65536u) ? p.offs2[gn] : 0u;
+#if GBSORT_MSD_LOCAL_L2
+        {  // the next group into L2 while this one sorts
+            const uintptr_t a = reinterpret_cast<uintptr_t>(keys + on) & ~uintptr_t(127);
+            const uintptr_t e = reinterpret_cast<uintptr_t>(keys + on + cn);
+            for (uintptr_t q = a + uintptr_t(tid) * 128; q < e; q += uintptr_t(THREADS) * 128)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+        }
+#endif
         if (c != 0u) {
             U* at = keys + o;
             static_assert(SPLIT_WORDS <= G::CTR_WORDS, "the split's counters");

@@ -22,6 +22,8 @@
 //     upsweep) serves every pass; all waits are bounded by %globaltimer.
 #pragma once
 
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "shapes.h"
 #include "sort_params.h"
@@ -87,46 +89,52 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
     __syncthreads();
 
     const int kind = p.kind, desc = p.desc;
-    auto count = [&](U k) {
-        const U t = twiddle_in<U>(k, kind, desc);
+    // every digit (the usual case, fully unrolled) or the digits in
+    // [dlo, dhi): the loop is compiled once for each
+    auto sweep = [&](auto all_digits) {
+        constexpr bool ALL = decltype(all_digits)::value;
+        auto count = [&](U k) {
+            const U t = twiddle_in<U>(k, kind, desc);
 #pragma unroll
-        for (int d = 0; d < G::P; ++d)
-            if (d >= dlo && d < dhi) atomicAdd(&cnt[(d * 256 + digit_of(t, d)) * G::COPIES + copy], 1u);
-    };
+            for (int d = 0; d < G::P; ++d)
+                if (ALL || (d >= dlo && d < dhi)) atomicAdd(&cnt[(d * 256 + digit_of(t, d)) * G::COPIES + copy], 1u);
+        };
+        const U* keys = static_cast<const U*>(p.keys);
+        const uint64_t n = p.n;
+        const uintptr_t addr = reinterpret_cast<uintptr_t>(keys);
+        uint64_t head = ((16u - (addr & 15u)) & 15u) / KB;
+        if (head > n) head = n;
+        const uint64_t nvec = (n - head) * KB / 16;
+        constexpr int PER_VEC = 16 / KB;
+        const uint64_t gthreads = uint64_t(gridDim.x) * HIST_THREADS;
+        const uint64_t gtid = uint64_t(blockIdx.x) * HIST_THREADS + tid;
 
-    const U* keys = static_cast<const U*>(p.keys);
-    const uint64_t n = p.n;
-    const uintptr_t addr = reinterpret_cast<uintptr_t>(keys);
-    uint64_t head = ((16u - (addr & 15u)) & 15u) / KB;
-    if (head > n) head = n;
-    const uint64_t nvec = (n - head) * KB / 16;
-    constexpr int PER_VEC = 16 / KB;
-    const uint64_t gthreads = uint64_t(gridDim.x) * HIST_THREADS;
-    const uint64_t gtid = uint64_t(blockIdx.x) * HIST_THREADS + tid;
-
-    if (gtid < head) count(keys[gtid]);
-    const uint4* vec = reinterpret_cast<const uint4*>(keys + head);
-    constexpr int UNROLL = 4;
-    uint64_t i = gtid;
-    for (; i + (UNROLL - 1) * gthreads < nvec; i += UNROLL * gthreads) {
-        uint4 v[UNROLL];
+        if (gtid < head) count(keys[gtid]);
+        const uint4* vec = reinterpret_cast<const uint4*>(keys + head);
+        constexpr int UNROLL = 4;
+        uint64_t i = gtid;
+        for (; i + (UNROLL - 1) * gthreads < nvec; i += UNROLL * gthreads) {
+            uint4 v[UNROLL];
 #pragma unroll
-        for (int r = 0; r < UNROLL; ++r) v[r] = __ldcs(vec + i + r * gthreads);
+            for (int r = 0; r < UNROLL; ++r) v[r] = __ldcs(vec + i + r * gthreads);
 #pragma unroll
-        for (int r = 0; r < UNROLL; ++r) {
+            for (int r = 0; r < UNROLL; ++r) {
+                union { uint4 q; U k[PER_VEC]; } w;
+                w.q = v[r];
+#pragma unroll
+                for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
+            }
+        }
+        for (; i < nvec; i += gthreads) {
             union { uint4 q; U k[PER_VEC]; } w;
-            w.q = v[r];
+            w.q = __ldcs(vec + i);
 #pragma unroll
             for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
         }
-    }
-    for (; i < nvec; i += gthreads) {
-        union { uint4 q; U k[PER_VEC]; } w;
-        w.q = __ldcs(vec + i);
-#pragma unroll
-        for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
-    }
-    for (uint64_t j = head + nvec * PER_VEC + gtid; j < n; j += gthreads) count(keys[j]);
+        for (uint64_t j = head + nvec * PER_VEC + gtid; j < n; j += gthreads) count(keys[j]);
+    };
+    if (dlo == 0 && dhi == G::P) sweep(std::true_type{});
+    else sweep(std::false_type{});
     __syncthreads();
 
     // Reduce the copies: one warp per bin, conflict-free row read.

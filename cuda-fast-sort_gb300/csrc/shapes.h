@@ -111,6 +111,9 @@ struct MsdShape {
     static constexpr int C_MIN_CTAS[2] = {3, 2};
     static constexpr int C_SPLIT_WORDS[2] = {KB == 16 ? 2048 : 4096, 4096};
 };
+// (4-byte keys measured slower this way: 2^28 u32 5.12 vs 4.11 ms, 2^25
+// 1.01 vs 0.58 — groups of 4096 keys with 16 bits left cost their local sort
+// more than the two digit passes it replaces.)
 constexpr bool msd_key_bytes(int kb) { return kb == 8 || kb == 16; }
 constexpr uint64_t msd_n_min(int kb) { return kb == 16 ? uint64_t(1) << 22 : uint64_t(3) << 23; }
 constexpr uint64_t msd_n_max(int kb) { return kb == 16 ? uint64_t(1) << 27 : uint64_t(1) << 28; }
