@@ -19,11 +19,14 @@
 //                 exact ranges (alternate buffer -> caller's buffer);
 //   local sorts:  each CTA sorts whole groups in place in shared memory (the
 //                 bucket split of fused_short.cuh: a counting pass on the next
-//                 12 bits, then a comparison rank inside the sub-buckets; or a
-//                 ranked pass per remaining digit where a sub-bucket is big)
-//                 and writes them untwiddled.
+//                 11-12 bits, then a comparison rank inside the sub-buckets)
+//                 and writes them untwiddled; a group with a sub-bucket too
+//                 big for the comparison rank goes back untwiddled unsorted
+//                 and turns the state to MSD_OFF.
 // With MSD_OFF the least-significant-digit passes, launched after these
-// kernels, run from the untouched input; with MSD_OK they exit at once.
+// kernels, sort from the caller's buffer, which then holds the input's keys
+// in some order (untouched, or as the local sorts left them); with MSD_OK
+// they exit at once.
 // Every key is read and written three times (plus the upsweep's and the pair
 // count's reads): 16-byte keys 2^26 measured 0.38 ms per split against 0.54
 // ms per digit pass.
@@ -341,7 +344,7 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_second_kernel(MsdParams
 template <int KB, int THREADS, int LIPT>
 struct MsdLocalGeom {
     static constexpr int WARPS = THREADS / 32;
-    static constexpr int CTR_WORDS = 2 * WARPS * 256;  // the split's sub-buckets, or warp histograms + match words
+    static constexpr int CTR_WORDS = 2 * WARPS * 256;  // the split's sub-buckets
     static constexpr size_t BUF_BYTES = (size_t(THREADS) * LIPT * KB + 127) & ~size_t(127);
     static constexpr size_t CTR_OFF = BUF_BYTES;
     static constexpr size_t SCAN_OFF = CTR_OFF + size_t(CTR_WORDS) * 4;  // u32 [32]
@@ -407,10 +410,17 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_local_kernel(MsdParams 
                 cta_bucket_split<KB, THREADS, LIPT, SPLIT_WORDS, 8 * (KB - 2)>(k, at, c, smem, ctr, scan, misc, p.kind,
                                                                               p.desc);
             if (!split) {
-                cta_bucket_sort<KB, THREADS, LIPT>(at, at, c, KB - 2, smem, ctr, ctr + G::WARPS * 256, scan, p.kind,
-                                                   p.desc);
-                for (int i = tid; i < G::WARPS * 256; i += THREADS) ctr[i] = 0u;  // the split's counters
-                __syncthreads();
+                // a sub-bucket too big for the comparison rank (repeated
+                // keys): the group goes back untwiddled, like every group
+                // sorted here, so the buffer holds the input's keys in some
+                // order, and the digit passes sort it (keys only: any order
+                // of the input sorts to the same bytes)
+#pragma unroll
+                for (int u = 0; u < LIPT; ++u) {
+                    const uint32_t j = uint32_t(u * THREADS + tid);
+                    if (j < c) at[j] = twiddle_out<U>(k[u], p.kind, p.desc);
+                }
+                if (tid == 0) *p.state = MSD_OFF;
             }
         }
         load(cn, on);

@@ -9,8 +9,9 @@ split, in-place local sorts of the (top, second) digit groups.
   - the input-preserving and DoubleBuffer forms;
   - inputs whose groups outgrow a local sort (keys sharing their top 16
     bits, a few distinct top-16-bit prefixes) fall back to the digit passes
-    on the device; repeated keys (ties inside sub-buckets, and sub-buckets
-    too big for the comparison rank);
+    on the device, and so does a group whose local sort gives up (a
+    sub-bucket too big for the comparison rank), from the keys as the local
+    sorts left them; repeated keys;
   - the timed sort reports the six kernels between the histogram and the
     digit passes.
 """
@@ -120,6 +121,41 @@ def test_big_groups_fall_back_to_the_digit_passes(gb, cuda, oracle, msd_on, kt, 
     on, off = _both(gb, cuda, kt, raw, False)
     assert _eq(on, oracle.sort(kt, raw, False))
     assert _eq(on, off)
+
+
+def _crowd_one_sub_bucket(kt, raw, count, seed):
+    """`count` keys get the same top 28 bits: their group still fits a local
+    sort, but one of its sub-buckets holds far more keys than the comparison
+    rank takes, so that group's local sort gives up and the digit passes sort
+    the whole array from what the local sorts left."""
+    out = raw.copy()
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(raw.shape[0], count, replace=False)
+    top = np.uint64(0xABCDEF1) << np.uint64(36)
+    low = np.uint64((1 << 36) - 1)
+    if KEY_BYTES[kt] == 16:
+        h = out.view(np.uint64).reshape(-1, 2)  # little-endian: column 1 holds the top bytes
+        h[idx, 1] = (h[idx, 1] & low) | top
+    else:
+        out[idx] = (out[idx] & low) | top
+    return out
+
+
+@pytest.mark.parametrize("kt", ["f128", "i64", "u128", "f64"])
+def test_a_local_sort_that_gives_up(gb, cuda, oracle, msd_on, kt):
+    n = N16 if KEY_BYTES[kt] == 16 else N8
+    raw = _crowd_one_sub_bucket(kt, raw_keys(kt, n, seed=61), 200, seed=62)
+    on, off = _both(gb, cuda, kt, raw, True)
+    assert _eq(on, oracle.sort(kt, raw, True))
+    assert _eq(on, off)
+    # the input-preserving form sorts from its untouched input
+    src = to_dev(cuda, raw)
+    out = cuda.zeros_like(src)
+    tb = gb.temp_bytes(kt, n)
+    ws = cuda.empty(tb, dtype=cuda.uint8, device="cuda")
+    gb.sort_copy(src, out, n, kt, ws, tb, descending=True)
+    cuda.cuda.synchronize()
+    assert _eq(from_dev(out, raw), on)
 
 
 @pytest.mark.parametrize("kt,distinct", [("u64", 1 << 20), ("u64", 1 << 13), ("u128", 1 << 19)])
