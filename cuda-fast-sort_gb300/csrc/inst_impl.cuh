@@ -77,7 +77,7 @@ const KernelEntry* msd_entries_for() {
         {reinterpret_cast<const void*>(&msd_top_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
          GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
         {reinterpret_cast<const void*>(&msd_count_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
-         GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
+         GS::TILE, static_cast<unsigned long>(MsdCountGeom<KB, S::THREADS, S::IPT>::SMEM_BYTES)},
         {reinterpret_cast<const void*>(&msd_scan_kernel<KB>), MSD_SCAN_THREADS, 0, 0, 0ul},
         {reinterpret_cast<const void*>(&msd_second_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
          GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},

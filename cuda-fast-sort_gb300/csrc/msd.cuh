@@ -219,11 +219,19 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_top_kernel(MsdParams p)
     }
 }
 
-// Pair count: keys per (top, second) digit.
+// Pair count: keys per (top, second) digit.  Its shared memory is the
+// words of the split's layout only (no stage).
+template <int KB, int THREADS, int IPT>
+struct MsdCountGeom {
+    static constexpr int TILE = THREADS * IPT;
+    static constexpr size_t WORDS_OFF = 0;
+    static constexpr size_t SMEM_BYTES = MsdSplitGeom<KB, THREADS, IPT>::SMEM_BYTES -
+                                         MsdSplitGeom<KB, THREADS, IPT>::WORDS_OFF;
+};
 template <int KB, int THREADS, int IPT, int MIN_CTAS>
 __global__ void __launch_bounds__(THREADS, MIN_CTAS) msd_count_kernel(MsdParams p) {
     using U = typename KeyBits<KB>::U;
-    using G = MsdSplitGeom<KB, THREADS, IPT>;
+    using G = MsdCountGeom<KB, THREADS, IPT>;
     extern __shared__ __align__(128) uint8_t smem[];
     uint32_t* bins = reinterpret_cast<uint32_t*>(smem + G::WORDS_OFF);
     uint32_t* tstart = bins + 512;

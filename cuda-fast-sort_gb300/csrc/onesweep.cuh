@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) upsweep_kernel(HistParams p) 
 
         if (gtid < head) count(keys[gtid]);
         const uint4* vec = reinterpret_cast<const uint4*>(keys + head);
-        constexpr int UNROLL = 4;
+        constexpr int UNROLL = 4;  // (8 for the top digit alone: u64 2^27 0.19 -> 0.28 ms)
         uint64_t i = gtid;
         for (; i + (UNROLL - 1) * gthreads < nvec; i += UNROLL * gthreads) {
             uint4 v[UNROLL];

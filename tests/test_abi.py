@@ -7,6 +7,8 @@ import subprocess
 
 import pytest
 
+from _oracle import KEY_BYTES
+
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(REPO, "include", "gbsort.h")
 
@@ -52,6 +54,27 @@ def test_size_query_needs_no_device(gb):
             b = gb.temp_bytes(kt, n)
             assert b >= prev
             prev = b
+
+
+def test_size_query_reserves_the_msd_blocks(gb):
+    """The size query holds room for the path a keys-only sort may take,
+    whether or not it is switched on: the one-launch sort's top-digit regions
+    (short arrays) and the MSD block of large 8- and 16-byte keys (state,
+    claim counters, 65536 group sizes, claims and offsets)."""
+    msd_block = 256 + 256 * 4 + 3 * 65536 * 4
+
+    def beyond_buffers(kt, n):  # bytes past the alternate keys and the lookback status
+        p = gb.plan(kt, n)
+        return gb.temp_bytes(kt, n) - n * KEY_BYTES[kt] - p.num_tiles * 256 * p.status_word_bytes
+
+    for kt, n in (("u64", 1 << 25), ("f128", 1 << 23), ("u128", 1 << 27)):
+        assert beyond_buffers(kt, n) >= msd_block
+    # 4-byte keys, pairs and sizes outside the range carry no MSD block
+    for kt, n in (("u32", 1 << 25), ("u64", 1 << 24), ("u128", (1 << 27) + 1)):
+        assert beyond_buffers(kt, n) < 64 << 10
+    # short keys-only arrays: the regions hold every key with a margin
+    n = 1 << 20
+    assert gb.temp_bytes("u32", n) >= 2 * n * 4
 
 
 def test_plan_reports_geometry(gb):
