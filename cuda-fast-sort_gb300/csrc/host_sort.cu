@@ -639,7 +639,11 @@ int gbsort_sort_host(int key_type, int descending, void* h_keys, void* h_values,
     if (!device_is_sm103()) return GBSORT_ERR_UNSUPPORTED;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint8_t* base = static_cast<uint8_t*>(d_buffer);
-    if (plan.passes >= 2 && n >= split_min_keys()) {
+    // the split path overlaps the copies with per-group digit passes; a
+    // keys-only sort that goes most significant digit first on the device
+    // is short enough that copy, sort, copy wins (2^26 u128: the device sort
+    // takes 2 ms of the ~12 the copies take)
+    if (plan.passes >= 2 && n >= split_min_keys() && !plan.msd) {
         SplitLayout L;
         st = split_layout(key_type, value_bytes, n, &L);
         if (st != GBSORT_OK) return st;

@@ -6,7 +6,8 @@ split, in-place local sorts of the (top, second) digit groups.
     range and not for pairs, narrower keys or sizes outside;
   - every 8- and 16-byte key type, both orders: equal to the oracle and to
     the digit passes (the path switched off);
-  - the input-preserving and DoubleBuffer forms;
+  - the input-preserving and DoubleBuffer forms, and the sort of a
+    host-memory array (copy, sort, copy back);
   - inputs whose groups outgrow a local sort (keys sharing their top 16
     bits, a few distinct top-16-bit prefixes) fall back to the digit passes
     on the device, and so does a group whose local sort gives up (a
@@ -181,3 +182,16 @@ def test_timed_entries(gb, cuda, msd_on):
     # histogram, 5 MSD kernels, the other digits' histogram, 16 passes (these two exit at once), fix-up
     assert len(ms) == info.kernel_launches
     assert all(t >= 0 for t in ms)
+
+
+@pytest.mark.parametrize("kt", ["u128", "i64"])
+def test_host_memory_sort(gb, cuda, oracle, msd_on, kt):
+    """gbsort_sort_host of a keys-only array in the MSD range: copy, sort
+    most significant digit first, copy back (instead of the split path)."""
+    n = N16 if KEY_BYTES[kt] == 16 else N8
+    raw = raw_keys(kt, n, seed=71)
+    hk = cuda.from_numpy(np.ascontiguousarray(raw).view(np.uint8).reshape(-1).copy()).pin_memory()
+    hb = gb.host_buffer_bytes(kt, n)
+    dbuf = cuda.empty(hb, dtype=cuda.uint8, device="cuda")
+    gb.sort_host(hk.data_ptr(), n, kt, dbuf, hb, descending=True)
+    assert _eq(hk.numpy().view(raw.dtype).reshape(raw.shape), oracle.sort(kt, raw, True))
