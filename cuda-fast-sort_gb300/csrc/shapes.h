@@ -93,7 +93,7 @@ constexpr int fused_local_tile(int kb) {
 // (msd.cuh): the two splits' tiles (THREADS x IPT keys; 8-byte keys 2^27:
 // 2.95 ms with 24 keys per thread, 3.06 with 16, 3.03 with 32) and the local
 // sorts' CTAs (groups of up to C_THREADS x C_LIPT keys), for n in
-// [msd_n_min, msd_n_max] (groups of ~64 to ~2048 / ~384 to ~4096 keys;
+// [msd_n_min, msd_n_max] (groups of ~24 to ~2048 / ~384 to ~4096 keys;
 // outside, the digit passes).  Measured against the digit passes, CUDA
 // events, descending: 16-byte keys 2^22 0.58 vs 0.82 ms, 2^24 0.89 vs 2.46,
 // 2^26 2.11 vs 9.24; 8-byte keys 2^24 0.86 vs 0.82, 2^25 1.18 vs 1.52, 2^27
@@ -115,7 +115,10 @@ struct MsdShape {
 // 1.01 vs 0.58 — groups of 4096 keys with 16 bits left cost their local sort
 // more than the two digit passes it replaces.)
 constexpr bool msd_key_bytes(int kb) { return kb == 8 || kb == 16; }
-constexpr uint64_t msd_n_min(int kb) { return kb == 16 ? uint64_t(1) << 22 : uint64_t(3) << 23; }
+// (16-byte keys, descending, against the digit passes of the short shape:
+// 2^20 0.40 vs 0.32 ms, 1.5 x 2^20 0.488 vs 0.491, 2^21 0.50 vs 0.56, 3 x 2^20
+// 0.52 vs 0.74.)
+constexpr uint64_t msd_n_min(int kb) { return kb == 16 ? uint64_t(3) << 19 : uint64_t(3) << 23; }
 constexpr uint64_t msd_n_max(int kb) { return kb == 16 ? uint64_t(1) << 27 : uint64_t(1) << 28; }
 // the local-sort shape for n keys (groups of n / 65536 on average)
 constexpr int msd_local_shape(int kb, uint64_t n) { return n <= (msd_n_max(kb) >> 1) ? 0 : 1; }

@@ -329,11 +329,11 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
             off = align_up(off + size_t(256) * p.msd_cap * kb, 256);
         }
     }
-    // keys-only sorts of 8- and 16-byte keys above the short range: the MSD
-    // block (sized whether or not the path is switched on), right after the
-    // status words so that the upsweep clears both in one sweep
-    if (!small && p.vb == 0 && msd_key_bytes(p.kb) && n >= msd_n_min(p.kb) && n <= msd_n_max(p.kb) &&
-        msd_entries(p.kb) != nullptr) {
+    // keys-only sorts of 8- and 16-byte keys above the one-launch range: the
+    // MSD block (sized whether or not the path is switched on), right after
+    // the status words so that the upsweep clears both in one sweep
+    if ((!small || n > fused_n_max(p.kb)) && p.vb == 0 && msd_key_bytes(p.kb) && n >= msd_n_min(p.kb) &&
+        n <= msd_n_max(p.kb) && msd_entries(p.kb) != nullptr) {
         p.msd_off = off;
         off = align_up(off + MsdLayout::BYTES, 256);
         const int shape = msd_local_shape(p.kb, n);

@@ -477,7 +477,8 @@ void gbsort_set_short_msd(int enable);
 int gbsort_get_short_msd(void);
 
 /* Keys-only sorts of 8- and 16-byte keys above the short range (1.5 x 2^24
- * to 2^28 keys of 8 bytes, 2^22 to 2^27 of 16): most significant digit first —
+ * to 2^28 keys of 8 bytes, 1.5 x 2^20 to 2^27 of 16): most significant digit
+ * first —
  * a split by the top digit, a count of (top, second) digit pairs, a split by
  * the second digit into the 65536 pairs' ranges, and in-place local sorts
  * of those groups in shared memory — instead of one stable pass per key

@@ -60,6 +60,8 @@ def test_plan_reports_the_path(gb, msd_on):
     assert gb.plan("u64", N8, 8).msd_stages == 0      # pairs keep the stable passes
     assert gb.plan("u32", 1 << 24).msd_stages == 0    # 4-byte keys: digit passes
     assert gb.plan("u64", 1 << 24).msd_stages == 0    # below the range
+    assert gb.plan("u128", 1 << 20).msd_stages == 0   # the one-launch sort's
+    assert gb.plan("u128", 3 << 19).msd_stages == 6
     assert gb.plan("u128", (1 << 27) + 1).msd_stages == 0  # above it
     tb = gb.temp_bytes("u64", N8)
     gb.set_msd(False)
@@ -195,3 +197,20 @@ def test_host_memory_sort(gb, cuda, oracle, msd_on, kt):
     dbuf = cuda.empty(hb, dtype=cuda.uint8, device="cuda")
     gb.sort_host(hk.data_ptr(), n, kt, dbuf, hb, descending=True)
     assert _eq(hk.numpy().view(raw.dtype).reshape(raw.shape), oracle.sort(kt, raw, True))
+
+
+@pytest.mark.parametrize("kt", ["u128", "f128"])
+def test_lower_end_of_the_range(gb, cuda, oracle, msd_on, kt):
+    """16-byte keys just above the one-launch sort's range: the MSD path,
+    with the short tile shape for its fallback passes; equal to the oracle
+    and to those passes, also when a group is too big."""
+    n = (3 << 19) + 7
+    assert gb.plan(kt, n).msd_stages == 6
+    raw = raw_keys(kt, n, seed=81)
+    on, off = _both(gb, cuda, kt, raw, True)
+    assert _eq(on, oracle.sort(kt, raw, True))
+    assert _eq(on, off)
+    raw = _top16_prefixes(kt, raw, [0x4321], seed=4)
+    on, off = _both(gb, cuda, kt, raw, False)
+    assert _eq(on, oracle.sort(kt, raw, False))
+    assert _eq(on, off)
