@@ -77,6 +77,27 @@ def test_size_query_reserves_the_msd_blocks(gb):
     assert gb.temp_bytes("u32", n) >= 2 * n * 4
 
 
+def test_msd_planning_needs_no_device(gb):
+    """Which keys-only sorts go most significant digit first (host logic):
+    8-byte keys from 1.5 x 2^24 to 2^28, 16-byte keys from 1.5 x 2^20 to
+    2^27, never pairs or narrower keys; the switch changes the plan, not the
+    size query."""
+    assert gb.get_msd()
+    for kt, n, want in (("u64", 3 << 23, 6), ("i64", 1 << 28, 6), ("f64", (3 << 23) - 1, 0),
+                        ("u64", (1 << 28) + 1, 0), ("u128", 3 << 19, 6), ("f128", 1 << 27, 6),
+                        ("i128", (3 << 19) - 1, 0), ("u128", (1 << 27) + 1, 0), ("u32", 1 << 26, 0),
+                        ("u16", 1 << 26, 0)):
+        assert gb.plan(kt, n).msd_stages == want, (kt, n)
+    assert gb.plan("u64", 1 << 26, 8).msd_stages == 0
+    tb = gb.temp_bytes("u128", 1 << 24)
+    gb.set_msd(False)
+    try:
+        assert gb.plan("u128", 1 << 24).msd_stages == 0
+        assert gb.temp_bytes("u128", 1 << 24) == tb
+    finally:
+        gb.set_msd(True)
+
+
 def test_plan_reports_geometry(gb):
     p = gb.plan("u32", 1 << 28)
     assert p.passes == 4 and p.radix_bits == 8
