@@ -107,8 +107,11 @@ struct MsdShape {
     static constexpr int IPT = KB == 16 ? 12 : 24;
     static constexpr int MIN_CTAS = 2;
     static constexpr int C_THREADS = 256;
-    static constexpr int C_LIPT[2] = {KB == 16 ? 8 : 12, KB == 16 ? 12 : 24};
-    static constexpr int C_MIN_CTAS[2] = {3, 2};
+    // 16-byte keys up to 2^26 (groups of up to ~1024 keys on average): 6 keys
+    // a thread, 4 CTAs an SM (2^26: local sorts 0.655 ms against 0.703 with
+    // 8 keys a thread and 3 CTAs; 1024 sub-buckets 0.694)
+    static constexpr int C_LIPT[2] = {KB == 16 ? 6 : 12, KB == 16 ? 12 : 24};
+    static constexpr int C_MIN_CTAS[2] = {KB == 16 ? 4 : 3, 2};
     static constexpr int C_SPLIT_WORDS[2] = {KB == 16 ? 2048 : 4096, 4096};
 };
 // (4-byte keys measured slower this way: 2^28 u32 5.12 vs 4.11 ms, 2^25
