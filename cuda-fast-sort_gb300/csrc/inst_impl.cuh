@@ -58,7 +58,7 @@ const KernelEntry* fused_entry_for() {
 
 // Keys-only sorts of 8- and 16-byte keys, most significant digit first:
 // top split, pair count, scan, second split, local sorts (shape 0), local
-// sorts (shape 1).
+// sorts (shape 1), the top digit's histogram.
 template <int KB, int L>
 KernelEntry make_msd_local_entry() {
     using S = MsdShape<KB>;
@@ -73,7 +73,7 @@ template <int KB>
 const KernelEntry* msd_entries_for() {
     using S = MsdShape<KB>;
     using GS = MsdSplitGeom<KB, S::THREADS, S::IPT>;
-    static const KernelEntry e[6] = {
+    static const KernelEntry e[7] = {
         {reinterpret_cast<const void*>(&msd_top_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
          GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
         {reinterpret_cast<const void*>(&msd_count_kernel<KB, S::THREADS, S::IPT, S::MIN_CTAS>), S::THREADS, S::IPT,
@@ -83,6 +83,7 @@ const KernelEntry* msd_entries_for() {
          GS::TILE, static_cast<unsigned long>(GS::SMEM_BYTES)},
         make_msd_local_entry<KB, 0>(),
         make_msd_local_entry<KB, 1>(),
+        {reinterpret_cast<const void*>(&msd_hist_kernel<KB>), MSD_HIST_THREADS, 0, 0, 0ul},
     };
     return e;
 }

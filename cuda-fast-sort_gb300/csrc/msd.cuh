@@ -52,6 +52,69 @@ struct MsdParams {
     uint32_t* err;         // workspace error word
 };
 
+// The MSD path's first kernel: the top digit's counts of the input into
+// h.gp_counts (the row of digit P-1), and the clear of the status words and
+// the MSD block (h.status, h.status_bytes).  One digit needs 256 counters
+// (32 copies, one per lane: no same-word atomics), so several CTAs fit an
+// SM and keep more loads in flight than the all-digit histogram kernel
+// (one CTA of 1024 threads an SM for its 128 KB of counters).
+constexpr int MSD_HIST_THREADS = 512;
+template <int KB>
+__global__ void __launch_bounds__(MSD_HIST_THREADS, 2) msd_hist_kernel(HistParams h) {
+    using U = typename KeyBits<KB>::U;
+    __shared__ uint32_t cnt[256 * 32];
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int i = tid; i < 256 * 32; i += MSD_HIST_THREADS) cnt[i] = 0u;
+    grid_launch_dependents();
+    {
+        const uint64_t nv = h.status_bytes >> 4;
+        uint4* st = static_cast<uint4*>(h.status);
+        const uint64_t stride = uint64_t(gridDim.x) * MSD_HIST_THREADS;
+        for (uint64_t i = uint64_t(blockIdx.x) * MSD_HIST_THREADS + tid; i < nv; i += stride)
+            st[i] = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    const U* keys = static_cast<const U*>(h.keys);
+    const uint64_t n = h.n;
+    auto count = [&](U k) { atomicAdd(&cnt[digit_of(twiddle_in<U>(k, h.kind, h.desc), KB - 1) * 32 + lane], 1u); };
+    uint64_t head = ((16u - (reinterpret_cast<uintptr_t>(keys) & 15u)) & 15u) / KB;
+    if (head > n) head = n;
+    const uint64_t nvec = (n - head) * KB / 16;
+    constexpr int PER_VEC = 16 / KB, UNROLL = 4;
+    const uint64_t gthreads = uint64_t(gridDim.x) * MSD_HIST_THREADS;
+    const uint64_t gtid = uint64_t(blockIdx.x) * MSD_HIST_THREADS + tid;
+    if (gtid < head) count(keys[gtid]);
+    const uint4* vec = reinterpret_cast<const uint4*>(keys + head);
+    uint64_t i = gtid;
+    for (; i + (UNROLL - 1) * gthreads < nvec; i += UNROLL * gthreads) {
+        uint4 v[UNROLL];
+#pragma unroll
+        for (int r = 0; r < UNROLL; ++r) v[r] = __ldcs(vec + i + r * gthreads);
+#pragma unroll
+        for (int r = 0; r < UNROLL; ++r) {
+            union { uint4 q; U k[PER_VEC]; } w;
+            w.q = v[r];
+#pragma unroll
+            for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
+        }
+    }
+    for (; i < nvec; i += gthreads) {
+        union { uint4 q; U k[PER_VEC]; } w;
+        w.q = __ldcs(vec + i);
+#pragma unroll
+        for (int e = 0; e < PER_VEC; ++e) count(w.k[e]);
+    }
+    for (uint64_t j = head + nvec * PER_VEC + gtid; j < n; j += gthreads) count(keys[j]);
+    __syncthreads();
+    // one warp per bin: the 32 copies summed by a shuffle reduction
+    for (int bin = tid >> 5; bin < 256; bin += MSD_HIST_THREADS / 32) {
+        uint32_t c = cnt[bin * 32 + lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0 && c) atomicAdd(&h.gp_counts[size_t(KB - 1) * 256 + bin], static_cast<unsigned long long>(c));
+    }
+}
+
 // One tile split by one digit: `cnt` keys at src (twiddled on load when
 // TWIDDLE) go to dst at base[d] + (their place among the keys of digit d
 // that every tile claims from claim[d]), d = the key's digit `q`.  No order

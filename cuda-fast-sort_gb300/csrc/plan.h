@@ -85,6 +85,7 @@ struct Plan {
     // the upsweep — then group offsets [65536]
     bool msd = false;
     KernelEntry msd_k[5]{};
+    KernelEntry msd_hist{};  // its first kernel: the top digit's histogram
     uint32_t msd_group_cap = 0;
     size_t msd_off = 0;
     size_t total_bytes = 0;

@@ -342,6 +342,7 @@ int make_plan(int key_type, size_t value_bytes, uint64_t n, Plan* plan) {
             p.msd = true;
             for (int i = 0; i < 4; ++i) p.msd_k[i] = msd_entries(p.kb)[i];
             p.msd_k[4] = msd_entries(p.kb)[4 + shape];
+            p.msd_hist = msd_entries(p.kb)[6];
         }
     }
     p.total_bytes = off;
@@ -366,7 +367,7 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     st = prepare_kernel(plan.upsweep);
     if (st != GBSORT_OK) return st;
     // the MSD path of keys-only sorts runs when all its kernels can
-    bool use_msd = plan.msd;
+    bool use_msd = plan.msd && prepare_kernel(plan.msd_hist) == GBSORT_OK;
     for (int i = 0; use_msd && i < 5; ++i) use_msd = prepare_kernel(plan.msd_k[i]) == GBSORT_OK;
     const int ms_stages = use_msd ? 6 : 0;  // its five kernels and the other digits' histogram
 
@@ -538,8 +539,14 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     {
         void* args[] = {&hp};
         if (timed) cudaEventRecord(ev[0], stream);
-        e = cudaLaunchKernel(plan.upsweep.fn, dim3(hist_ctas), dim3(plan.upsweep.threads), args,
-                             plan.upsweep.smem, stream);
+        if (use_msd) {  // the top digit alone, several CTAs an SM
+            const int occ_h = resident_ctas(plan.msd_hist);
+            const uint32_t g = uint32_t((sms > 0 ? sms : 1) * (occ_h > 0 ? occ_h : 1));
+            e = cudaLaunchKernel(plan.msd_hist.fn, dim3(g), dim3(plan.msd_hist.threads), args, 0, stream);
+        } else {
+            e = cudaLaunchKernel(plan.upsweep.fn, dim3(hist_ctas), dim3(plan.upsweep.threads), args,
+                                 plan.upsweep.smem, stream);
+        }
         if (e != cudaSuccess) return fail("upsweep launch", e);
         if (timed) cudaEventRecord(ev[1], stream);
     }
