@@ -553,7 +553,9 @@ int enqueue_sort(const Plan& plan, int descending, void* d_keys, void* d_values,
     if (use_msd) {
         // Keys only, 8- or 16-byte keys: top split, pair count, scan, second
         // split, local sorts (msd.cuh); the digit passes below exit at once
-        // when these sorted, and sort from the untouched input otherwise.
+        // when these sorted, and otherwise sort from the input-preserving
+        // source or from the caller's buffer, which then holds the input's
+        // keys in some order (keys only: the same bytes come out).
         MsdParams mp{};
         mp.keys_in = copy ? keys_src : d_keys;
         mp.keys_a = d_keys;
